@@ -1,0 +1,386 @@
+"""ORACLE — test infrastructure only.
+
+CPU FP64 restatement of SCCM's PNAMP per-point algorithm, used by the tests,
+`__graft_entry__.smoke()` and the CPU leg of `bench.py` as the checker. The
+product path (the CUDA library behind `include/pnamp_gpu.h`) never imports or
+calls anything in this directory.
+
+It follows the reference call sequence literally (per-point ZGEMM / LU-inverse
+/ Pfaffian, sparse energy loop), not the GPU's algebraically reorganised form,
+so a GPU-vs-oracle comparison checks the reorganisation as well as the kernels.
+
+Parity pins: the axial path reproduces the reference's own Ge76 output files
+`data/Ge/kern.1D.*.elem` (tests/test_oracle_golden.py). The triaxial Pfaffian
+path has no reference output to pin against; it is cross-checked by invariants
+(N = 1 at the identity for q = q', Pf^2 = det, Hermiticity of N^J, agreement of
+the Pfaffian and Onishi norms where the Onishi sign is unambiguous).
+
+Reference files (paths inside jmyao17/SCCM):
+  PNAMP_Kernel3D.f90   mesh loop, norm assembly, projection      (Codes/PNAMP)
+  PNAMP_Kernel3D_v2.f90:477-498  plain D-function projection
+  PNAMP_Kernel1D.f90   axial loop (Onishi norm) and K=0 projection
+  PNAMP_Proj.f90       zbareover, ROTATION_MAT, Pfaf_Over, ZPfaffianF, ZExch,
+                       UVphiomega, ROKAPPAphiomega
+  PNAMP_Energy_OpenMP.f90  HFB_Energy_COMPLEX
+  PNAMP_ME1B.f90       ZN_0, ZQ2, ZQ2t
+  PNAMP_ME2B.f90       ZJ2_0
+  PNAMP_Onishi.f90     Onishi
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from sccm_gb300.basis import JJMAX, NOBS, CHOP, ModelSpace, Mesh, dwig
+
+
+@dataclass
+class Hamiltonian:
+    """Inputs the reference keeps in module `H` (VAPHFB_Par.f90:45-54)."""
+    e0: float
+    t1b: np.ndarray          # zME1BM, n x n, [row, col]
+    recs: np.ndarray         # (nrec, 4) 0-based a < b, c < d
+    vbar: np.ndarray         # (nrec,) antisymmetrised m-scheme V
+    q2: np.ndarray           # (5, n, n) Q_{2mu}, mu = -2..2
+    jops: tuple              # Jx, Jy, Jz, Jx^2, Jy^2, Jz^2
+
+
+# ---------------------------------------------------------------- per pair
+def zbareover(V, U):
+    """PNAMP_Proj.f90:6-79. Returns (ZZc = conj(V U^-1), Det = exp(-1/4 sum log(1+lam)))."""
+    uinv = np.linalg.inv(U.astype(complex))             # ZGETRF + ZGETRI
+    zz = V.astype(complex) @ uinv                        # Z* = V U^-1
+    zzc = np.conj(zz)
+    zztz = zzc.T @ zzc
+    lam = np.linalg.eigvals(zztz)                        # ZGEEV
+    ztest = np.sum(np.log(1.0 + lam))
+    return zzc, float(np.real(np.exp(-ztest / 4.0)))
+
+
+# ---------------------------------------------------------------- per Euler
+def rotation_mat(sp: ModelSpace, alp, bet, gam):
+    """PNAMP_Proj.f90:83-136: R(a,b) = e^{-i alp m_a} e^{-i gam m_b} d^{j}_{m_a m_b}(bet)."""
+    n = sp.nlev
+    R = np.zeros((n, n), complex)
+    for s, d in sp.blocks():
+        tj = int(sp.twoj[s])
+        for i in range(d):
+            ma = int(sp.twom[s + i])
+            for k in range(d):
+                mb = int(sp.twom[s + k])
+                R[s + i, s + k] = (np.exp(-1j * alp * ma / 2.0) * np.exp(-1j * gam * mb / 2.0)
+                                   * dwig(tj, ma, mb, bet))
+    return R
+
+
+def gauge_matrix(R, phip, phin):
+    """ZAM_PHI_OMEGA of UVphiomega (PNAMP_Proj.f90:413-439): species blocks of R times e^{i phi}."""
+    n = R.shape[0]
+    h = n // 2
+    A = np.zeros_like(R)
+    A[:h, :h] = np.exp(1j * phip) * R[:h, :h]
+    A[h:, h:] = np.exp(1j * phin) * R[h:, h:]
+    return A
+
+
+def uvphiomega(A, U1, V1):
+    """PNAMP_Proj.f90:441-452: Ubar = A U1, Vbar = conj(A) V1."""
+    return A @ U1, np.conj(A) @ V1
+
+
+# ---------------------------------------------------------------- Pfaffian
+def zpfaffian(SK, epsln=1.0e-13):
+    """ZPfaffianF (PNAMP_Proj.f90:218-350) with ZExch (:356-392).
+
+    Skew-symmetric Pfaffian by 2x2-block elimination with a global argmax pivot
+    over the remaining upper triangle, scanned row by row (first maximum wins),
+    sign `phas` per exchange, and Pf = 0 as soon as |pivot| <= epsln. The matrix
+    is kept in full skew form; row+column exchanges are pure moves, so the upper
+    triangle matches the reference's upper-triangle storage value for value.
+    Returns (Pf, status) with status 1 when the epsln early exit fired.
+    """
+    A = np.array(SK, dtype=complex, copy=True)
+    N = A.shape[0]
+    if N % 2:
+        return 0.0 + 0.0j, 0
+    NB = N // 2
+    if NB == 1:
+        return complex(A[0, 1]), 0
+    pf = 1.0 + 0.0j
+    iu = None
+    for k in range(NB - 1):
+        r, c = 2 * k, 2 * k + 1
+        sub = np.abs(A[r:, r:])
+        m = sub.shape[0]
+        if iu is None or iu[0].size != m * (m - 1) // 2:
+            iu = np.triu_indices(m, 1)
+        flat = sub[iu]
+        pos = int(np.argmax(flat))
+        i1, i2 = r + int(iu[0][pos]), r + int(iu[1][pos])
+        phas = 1.0
+        if i1 == r:
+            phas = -phas
+        if i2 == c:
+            phas = -phas
+        if i1 != r:
+            A[[r, i1], :] = A[[i1, r], :]
+            A[:, [r, i1]] = A[:, [i1, r]]
+        if i2 != c:
+            A[[c, i2], :] = A[[i2, c], :]
+            A[:, [c, i2]] = A[:, [i2, c]]
+        ss = A[r, c]
+        if not abs(ss) > epsln:
+            return 0.0 + 0.0j, 1
+        if c + 1 < N:
+            a = A[c, c + 1:].copy()      # Sk(NC, i)
+            b = A[r, c + 1:].copy()      # Sk(NR, i)
+            upd = (np.outer(a, b) - np.outer(b, a)) / ss
+            blk = A[c + 1:, c + 1:]
+            tri = np.triu(np.ones(blk.shape, bool), 1)
+            blk[tri] = blk[tri] + upd[tri]
+            lowt = np.tril(np.ones(blk.shape, bool), -1)
+            blk[lowt] = -blk.T[lowt]
+            np.fill_diagonal(blk, 0.0)
+            A[c + 1:, c + 1:] = blk
+        pf = pf * ss * phas
+    pf = pf * A[N - 2, N - 1]
+    return complex(pf), 0
+
+
+def pfaf_over(zzc0, Ubar, Vbar, cscale=1.0):
+    """PNAMP_Proj.f90:142-211: Pf( Cscale * [[conj(Vbar) conj(Ubar)^-1, -I], [I, -ZZc0]] )."""
+    n = Ubar.shape[0]
+    m1 = np.conj(Vbar) @ np.linalg.inv(np.conj(Ubar))
+    S = np.zeros((2 * n, 2 * n), complex)
+    S[:n, :n] = m1
+    S[n:, n:] = -zzc0
+    S[:n, n:] = -np.eye(n)
+    S[n:, :n] = np.eye(n)
+    S *= cscale
+    return zpfaffian(S)
+
+
+# ---------------------------------------------------------------- densities
+def rokappa(A, U0, V0, U1, V1):
+    """ROKAPPAphiomega (PNAMP_Proj.f90:459-551)."""
+    Ac = np.conj(A)
+    t22 = V0.T @ A @ V1 + U0.T @ Ac @ U1
+    t22inv = np.linalg.inv(t22)
+    aux1 = A @ V1
+    aux2 = -(Ac @ U1)
+    aux3 = t22inv @ V0.T
+    aux4 = t22inv @ U0.T
+    return aux1 @ aux3, aux1 @ aux4, aux2 @ aux3
+
+
+def zn0(rho):
+    """ZN_0 (PNAMP_ME1B.f90:218-237): proton (first half) and neutron traces."""
+    h = rho.shape[0] // 2
+    return np.trace(rho[:h, :h]), np.trace(rho[h:, h:])
+
+
+def energy(rho, k10, k01, ham: Hamiltonian):
+    """HFB_Energy_COMPLEX (PNAMP_Energy_OpenMP.f90:31-90). Returns (Ekin, Etot)."""
+    i, j, k, l = (ham.recs[:, q] for q in range(4))
+    R = rho
+    z_ijkl = R[k, i] * R[l, j] - R[l, i] * R[k, j] + k01[i, j] * k10[k, l]
+    z_jikl = R[k, j] * R[l, i] - R[l, j] * R[k, i] + k01[j, i] * k10[k, l]
+    z_jilk = R[l, j] * R[k, i] - R[k, j] * R[l, i] + k01[j, i] * k10[l, k]
+    z_ijlk = R[l, i] * R[k, j] - R[k, i] * R[l, j] + k01[i, j] * k10[l, k]
+    z_klij = R[i, k] * R[j, l] - R[j, k] * R[i, l] + k01[k, l] * k10[i, j]
+    z_klji = R[j, k] * R[i, l] - R[i, k] * R[j, l] + k01[k, l] * k10[j, i]
+    z_lkij = R[i, l] * R[j, k] - R[j, l] * R[i, k] + k01[l, k] * k10[i, j]
+    z_lkji = R[j, l] * R[i, k] - R[i, l] * R[j, k] + k01[l, k] * k10[j, i]
+    d = np.where(k + l == i + j, 0.0, 1.0)
+    e2 = np.sum(0.25 * ham.vbar * (z_ijkl + d * z_klij - z_jikl - d * z_klji
+                                   - z_ijlk - d * z_lkij + z_jilk + d * z_lkji))
+    ekin = np.sum(R.T * ham.t1b)           # sum_{a,c} rho(c,a) t(a,c)
+    return ekin, e2 + ekin
+
+
+def zj2(rho, k10, k01, jops):
+    """ZJ2_0 (PNAMP_ME2B.f90:1-152): <J^2> from J_i, J_i^2 traces."""
+    JX, JY, JZ, JX2, JY2, JZ2 = jops
+    tot = 0.0 + 0.0j
+    for J, J2 in ((JX, JX2), (JY, JY2), (JZ, JZ2)):
+        a1 = J2 @ rho
+        a2 = J @ rho
+        a3 = J @ k10
+        a4 = J.T @ k01.T
+        tot += np.trace(a1) + np.trace(a2) ** 2 - np.trace(a2 @ a2) + np.trace(a3 @ a4)
+    return tot
+
+
+def zq2(Q, rho):
+    """ZQ2 (PNAMP_ME1B.f90:52-79): proton trace of Q rho."""
+    h = rho.shape[0] // 2
+    aux = Q @ rho
+    return np.trace(aux[:h, :h]), np.trace(aux[h:, h:])
+
+
+def zq2t(Q, rho):
+    """ZQ2t (PNAMP_ME1B.f90:112-132): proton trace of Q^dagger rho."""
+    h = rho.shape[0] // 2
+    aux = np.conj(Q).T @ rho
+    return np.trace(aux[:h, :h]), np.trace(aux[h:, h:])
+
+
+def onishi(U0, V0, Ubar, Vbar):
+    """Onishi (PNAMP_Onishi.f90:1-37): sqrt(det(Ubar^T U0 + Vbar^T V0)), principal branch."""
+    b = Ubar.T @ U0 + Vbar.T @ V0
+    return complex(np.sqrt(np.linalg.det(b) + 0j))
+
+
+# ---------------------------------------------------------------- one point
+def point_observables(sp, ham, A, U0, V0, U1, V1, znorm, iE2=True):
+    """Observables 2..18 for one gauge point, weighted by the norm (Kernel3D.f90:296-358)."""
+    out = np.zeros(NOBS, complex)
+    rho, k10, k01 = rokappa(A, U0, V0, U1, V1)
+    zp, zn = zn0(rho)
+    out[0] = znorm
+    out[1] = znorm * zp
+    out[2] = znorm * zn
+    ekin, ehfb = energy(rho, k10, k01, ham)
+    out[3] = znorm * ekin
+    out[6] = znorm * (ehfb + ham.e0)
+    out[7] = znorm * zj2(rho, k10, k01, ham.jops)
+    if iE2:
+        for mu in range(5):
+            out[8 + mu] = znorm * zq2(ham.q2[mu], rho)[0]
+            out[13 + mu] = znorm * zq2t(ham.q2[mu], rho)[0]
+    return out
+
+
+def kernel_triaxial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1,
+                    cscale=1.0, iscale=0, iE2=True, euler_subset=None, point_log=None):
+    """Kernel4Triaxial mesh loop (PNAMP_Kernel3D.f90:70-407) -> ZRES[P_E, NOBS].
+
+    Shell-model runs always take the Pfaffian branch (ide forced to 1,
+    Kernel3D.f90:140-159). `euler_subset` restricts the loop to a list of Euler
+    indices (rows of ZRES left zero elsewhere) so tests can sample large meshes.
+    """
+    n = sp.nlev
+    U0, V0, U1, V1 = (np.asarray(x, dtype=float) for x in (U0, V0, U1, V1))
+    aaa = n * (n + 1) // 2
+    snpfaf = -1.0 if aaa % 2 else 1.0
+    zzc0, det0 = zbareover(V0, U0)
+    _zzc1, det1 = zbareover(V1, U1)
+    scale = 10.0 ** (-(n * iscale // 2))
+    zdv0, zdv1 = det0 * scale, det1 * scale
+    pts = mesh.euler_points()
+    phis = mesh.gauge_angles()
+    nf = mesh.nfom
+    zres = np.zeros((len(pts), NOBS), complex)
+    idx = range(len(pts)) if euler_subset is None else euler_subset
+    for ie in idx:
+        alp, bet, gam, _w = pts[ie]
+        R = rotation_mat(sp, alp, bet, gam)
+        acc = np.zeros(NOBS, complex)
+        for php in phis:
+            zph_p = np.exp(-1j * php * sp.nprot)
+            for phn in phis:
+                zph_n = np.exp(-1j * phn * sp.nneut)
+                A = gauge_matrix(R, php, phn)
+                ub, vb = uvphiomega(A, U1, V1)
+                pf, st = pfaf_over(zzc0, ub, vb, cscale)
+                znorm = snpfaf * zdv0 * zdv1 * pf * zph_p * zph_n
+                o = point_observables(sp, ham, A, U0, V0, U1, V1, znorm, iE2)
+                if point_log is not None:
+                    point_log.append((ie, php, phn, pf, o))
+                acc += o
+        zres[ie] = acc / nf ** 2
+    return zres
+
+
+def kernel_axial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1, iE2=True):
+    """Kernel4Axial mesh loop (PNAMP_Kernel1D.f90:190-426): Onishi norm at every gauge point."""
+    U0, V0, U1, V1 = (np.asarray(x, dtype=float) for x in (U0, V0, U1, V1))
+    pts = mesh.euler_points()
+    phis = mesh.gauge_angles()
+    nf = mesh.nfom
+    zres = np.zeros((len(pts), NOBS), complex)
+    for ie, (alp, bet, gam, _w) in enumerate(pts):
+        R = rotation_mat(sp, alp, bet, gam)
+        acc = np.zeros(NOBS, complex)
+        for php in phis:
+            zph_p = np.exp(-1j * php * sp.nprot)
+            for phn in phis:
+                zph_n = np.exp(-1j * phn * sp.nneut)
+                A = gauge_matrix(R, php, phn)
+                ub, vb = uvphiomega(A, U1, V1)
+                znorm = onishi(U0, V0, ub, vb)
+                acc += point_observables(sp, ham, A, U0, V0, U1, V1, znorm, iE2)
+        zres[ie] = acc / nf ** 2
+    return zres
+
+
+# ---------------------------------------------------------------- projection
+def projection_weights(mesh: Mesh, jmax=JJMAX):
+    """Plain D-function quadrature weights (PNAMP_Kernel3D_v2.f90:477-498).
+
+    W[J, K1+JJMAX, K2+JJMAX, ie] = weightJ * w_a w_b w_g e^{i K1 alp} d^J_{K1K2}(bet) e^{i K2 gam}
+    with weightJ = (2J+1)/(8 pi^2), or (2J+1)/2 when N_alp N_gam = 1 (Kernel3D.f90:78-81).
+    """
+    pts = mesh.euler_points()
+    W = np.zeros((jmax + 1, 2 * JJMAX + 1, 2 * JJMAX + 1, len(pts)), complex)
+    axial = mesh.nalp * mesh.ngam == 1
+    for J in range(0, jmax + 1):
+        wj = (2 * J + 1) / 2.0 if axial else (2 * J + 1) / (8 * math.pi ** 2)
+        for K1 in range(-J, J + 1):
+            for K2 in range(-J, J + 1):
+                for ie, (alp, bet, gam, w) in enumerate(pts):
+                    W[J, K1 + JJMAX, K2 + JJMAX, ie] = (wj * w * np.exp(1j * K1 * alp)
+                                                       * dwig(2 * J, 2 * K1, 2 * K2, bet)
+                                                       * np.exp(1j * K2 * gam))
+    return W
+
+
+def project(zres, mesh: Mesh, core_prot=0, core_neut=0, jmax=JJMAX, jstep=2, chop=CHOP):
+    """J/K projection of ZRES into the kernel-file fields (Kernel3D.f90:415-751, plain form).
+
+    Returns dict of arrays [J, K1+JJMAX, K2+JJMAX] for njkk, hjkk, nn, zz, J2
+    (only even J are filled: Kernel3D.f90:415). Fields below CHOP are left 0.
+    """
+    W = projection_weights(mesh, jmax)
+    S = np.einsum("jabe,eo->jabo", W, zres[:, :8])          # ZsumJKK(io, K1, K2)
+    shape = (JJMAX + 1, 2 * JJMAX + 1, 2 * JJMAX + 1)
+    out = {k: np.zeros(shape, complex) for k in ("njkk", "hjkk", "nn", "zz", "J2", "q0p", "q0pc")}
+    out["qpred"] = np.zeros(shape + (3,), complex)
+    out["qcpred"] = np.zeros(shape + (3,), complex)
+    out["zsum"] = S
+    for J in range(0, jmax + 1, jstep):
+        for K1 in range(-J, J + 1):
+            for K2 in range(-J, J + 1):
+                s = S[J, K1 + JJMAX, K2 + JJMAX]
+                if abs(s[0]) < chop:
+                    continue
+                ix = (J, K1 + JJMAX, K2 + JJMAX)
+                out["njkk"][ix] = s[0]
+                out["zz"][ix] = s[1] / s[0] + core_prot
+                out["nn"][ix] = s[2] / s[0] + core_neut
+                out["hjkk"][ix] = s[6]
+                out["J2"][ix] = s[7] / s[0]
+    return out
+
+
+def project_axial(zres, mesh: Mesh, core_prot=0, core_neut=0, jmax=JJMAX):
+    """K = 0 projection of the axial path (PNAMP_Kernel1D.f90:432-637): no CHOP."""
+    pts = mesh.euler_points()
+    shape = (JJMAX + 1, 2 * JJMAX + 1, 2 * JJMAX + 1)
+    out = {k: np.zeros(shape, complex) for k in ("njkk", "hjkk", "nn", "zz", "J2", "q0p", "q0pc")}
+    out["qpred"] = np.zeros(shape + (3,), complex)
+    out["qcpred"] = np.zeros(shape + (3,), complex)
+    o = JJMAX
+    for J in range(0, jmax + 1, 2):
+        wj = (2 * J + 1) / 2.0
+        s = np.zeros(8, complex)
+        for ie, (alp, bet, gam, w) in enumerate(pts):
+            s += wj * w * dwig(2 * J, 0, 0, bet) * zres[ie, :8]
+        out["nn"][J, o, o] = s[2] / s[0] + core_neut
+        out["zz"][J, o, o] = s[1] / s[0] + core_prot
+        out["hjkk"][J, o, o] = s[6]
+        out["njkk"][J, o, o] = s[0]
+        out["J2"][J, o, o] = s[7] / s[0]
+    return out
