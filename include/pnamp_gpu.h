@@ -1,0 +1,149 @@
+/*
+ * pnamp_gpu.h -- C ABI of the GB300 (sm_103a) PNAMP kernel library.
+ *
+ * Replaces the hot path of SCCM's PNAMP stage: the per-pair subroutine
+ *   subroutine Kernel4Triaxial(lpr, Nphi1, Nphi2, NLEV)
+ *     (Codes/PNAMP/PNAMP_Kernel3D.f90:1, called once per (q,q') pair from
+ *      Codes/PNAMP/PNAMP_Main.f90:113)
+ * and its per-point callees ROTATION_MAT, UVphiomega, Pfaf_Over/ZPfaffianF,
+ * ROKAPPAphiomega (Codes/PNAMP/PNAMP_Proj.f90:83-551), ZN_0/ZQ2/ZQ2t
+ * (PNAMP_ME1B.f90), ZJ2_0 (PNAMP_ME2B.f90) and HFB_Energy_COMPLEX
+ * (PNAMP_Energy_OpenMP.f90:5-100), followed by the J/K projection
+ * (PNAMP_Kernel3D.f90:415-751) whose result `post_general`/`post_axial`
+ * write to the kernel file (PNAMP_IO.f90:2-96).
+ *
+ * Conventions
+ *  - Plain C types only. Matrices are column-major like the Fortran arrays they
+ *    replace: element (i,j) of an n x n matrix is at [i + j*n].
+ *  - Complex numbers are interleaved (re, im) doubles, i.e. Fortran complex*16 /
+ *    C `double _Complex` layout.
+ *  - Every entry point returns a status code (0 = success) where the reference
+ *    `stop`s; `pnamp_strerror` gives the text. The library keeps no global
+ *    state: all state lives in a context, used by one host thread at a time.
+ *  - The caller owns every buffer passed in. The context owns its device memory.
+ *  - There is no CPU fallback: without a usable CUDA device `pnamp_init`
+ *    returns PNAMP_ERR_CUDA.
+ */
+#ifndef PNAMP_GPU_H
+#define PNAMP_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PNAMP_NOBS 19   /* observables per Euler point, NOBS (VAPHFB_Par.f90:168) */
+#define PNAMP_JJMAX 6   /* largest projected J, JJmax (VAPHFB_Par.f90:278) */
+#define PNAMP_NK (2 * PNAMP_JJMAX + 1)
+#define PNAMP_MAX_NLEV 64
+
+/* return codes */
+#define PNAMP_OK 0
+#define PNAMP_ERR_ARG 1          /* invalid argument (sizes, NULL pointers, model space) */
+#define PNAMP_ERR_CUDA 2         /* CUDA runtime error or no device */
+#define PNAMP_ERR_NOMEM 3        /* device allocation failed */
+#define PNAMP_ERR_SINGULAR_U 4   /* U of a vacuum is singular: zbareover/Pfaf_Over ZGETRF info != 0 */
+#define PNAMP_ERR_UNSUPPORTED 5  /* a size beyond what this build supports */
+#define PNAMP_ERR_STATE 6        /* call order violated */
+
+/* per-Euler-point status bits (OR over the gauge points of that Euler point) */
+#define PNAMP_ST_PIVOT_UNDERFLOW 1  /* Pfaffian pivot |ss| <= 1e-13: norm set to 0 (PNAMP_Proj.f90:290,333) */
+#define PNAMP_ST_SINGULAR_T22 2     /* exact zero pivot in the LU of T22 */
+#define PNAMP_ST_NONFINITE 4        /* a non-finite value reached ZRES */
+#define PNAMP_ST_SINGULAR_U 8       /* the pair's U0 or U1 is singular */
+
+/* Model space: the m-scheme `tnljm` arrays (VAPHFB_Par.f90:39-43), ordered
+ * protons (t = -1) first, then neutrons (t = +1); within a species orbits in
+ * .val order, m = j, j-1, ..., -j (Codes/GCM/HFBA_Hamiltonian.f90:43-68). */
+typedef struct {
+    int nlev;                     /* n = HO%NLEV, even, <= PNAMP_MAX_NLEV */
+    int nprot, nneut;             /* valence Z and N (Input%nprot, Input%nneut) */
+    int core_prot, core_neut;     /* Nucl%ncore(1), Nucl%ncore(0) */
+    const int *t, *n, *l, *twoj, *twom;   /* length nlev each */
+} pnamp_space;
+
+/* Hamiltonian and one-body operators (module H and cME1B, VAPHFB_Par.f90:45-81). */
+typedef struct {
+    double e0;                    /* H%E0 */
+    const double *t1b;            /* n x n single-particle matrix H%ME1BM */
+    int nrec;                     /* H%iabcd_max */
+    const int *ka, *kb, *kc, *kd; /* 1-based m-scheme indices, ka < kb, kc < kd, ka+kb <= kc+kd */
+    const double *vbar;           /* H%ME2BM, antisymmetrised m-scheme V */
+    const double *q2;             /* 5 blocks of n x n: Q_{2mu}, mu = -2..2 (cME1B%Q2_2t..Q22t);
+                                     NULL skips observables 9..18 (Input%iE2 = 0) */
+} pnamp_hamiltonian;
+
+/* Euler and gauge mesh (module AMP/PNP, VAPHFB_Par.f90:131-151; Codes/GCM/PNAMP_Gaus.f90). */
+typedef struct {
+    int nalp, nbet, ngam;         /* AMP%NLEG_ALP, NLEG_BET, NLEG_GAM */
+    int nfom;                     /* PNP%NFOM gauge points per species */
+    int ncosbet;                  /* 1, or 2 to use only the first nbet/2 beta nodes with doubled weight */
+    const double *alpha, *walp;   /* length nalp */
+    const double *beta, *wbet;    /* length nbet (beta = acos of the Gauss node) */
+    const double *gamma, *wgam;   /* length ngam */
+    double cscale;                /* Input%Cscale: Pfaffian matrix scale (PNAMP_Proj.f90:204-208) */
+    int iscale;                   /* Input%iscale: vacuum factor 10^(-NLEV*iscale/2) (Kernel3D.f90:149) */
+} pnamp_mesh;
+
+/* Projected kernels, the `Kernel%` fields consumed by post_general/post_axial
+ * (VAPHFB_Par.f90:281-290). Each array is complex [J][K1+JJMAX][K2+JJMAX],
+ * J = 0..JJMAX, with only even J filled (Kernel3D.f90:415); entries whose
+ * |N^J_{K1K2}| < CHOP = 1e-8 are 0 unless `chop` is 0. */
+typedef struct {
+    double *njkk, *hjkk, *nn, *zz, *j2;   /* each (JJMAX+1)*NK*NK complex */
+} pnamp_kernels;
+
+typedef struct pnamp_ctx pnamp_ctx;
+
+/* Set up a context: uploads the model space, Hamiltonian and mesh, builds the
+ * projection weights. Replaces the one-off part of PNAMP_Main.f90:27-50. */
+int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h,
+               const pnamp_mesh *m, pnamp_ctx **out);
+
+/* Number of Euler points P_E of the context's mesh (rows of ZRES). */
+int pnamp_n_euler(const pnamp_ctx *ctx);
+
+/* One (q, q') pair, host buffers: the mesh loop of Kernel4Triaxial
+ * (PNAMP_Kernel3D.f90:70-407). U0,V0 (bra q) and U1,V1 (ket q') are the real
+ * n x n HFB%U0.. arrays read from the .wf files. zres receives ZRES(P_E, NOBS)
+ * (column-major complex, ZRES(iang, io) at [iang + io*P_E]). point_status
+ * (length P_E) may be NULL. */
+int pnamp_pair(pnamp_ctx *ctx, const double *U0, const double *V0,
+               const double *U1, const double *V1, double *zres, int *point_status);
+
+/* A batch of pairs, host buffers. uv is [npairs][4][n*n]: U0, V0, U1, V1 of
+ * each pair, column-major; zres is [npairs][NOBS*P_E]; point_status is
+ * [npairs][P_E] or NULL. This is the cfg3-style batched entry the per-pair
+ * MPI round robin of PNAMP_Main.f90:79-84 feeds. */
+int pnamp_batch(pnamp_ctx *ctx, int npairs, const double *uv, double *zres, int *point_status);
+
+/* Same as pnamp_batch with DEVICE buffers, enqueued on `stream` (a
+ * cudaStream_t, NULL = legacy default stream); returns after the launch. */
+int pnamp_batch_device(pnamp_ctx *ctx, int npairs, const double *d_uv,
+                       double *d_zres, int *d_point_status, void *stream);
+
+/* J/K projection of one pair's ZRES into kernel-file fields (Kernel3D.f90:415-751,
+ * plain D-function form of PNAMP_Kernel3D_v2.f90:477-498; for an N_alp*N_gam = 1
+ * mesh the weight is (2J+1)/2 as in Kernel3D.f90:80). Host buffers. */
+int pnamp_project(pnamp_ctx *ctx, const double *zres, int chop, pnamp_kernels *out);
+
+/* Batched projection with DEVICE buffers: d_zres as from pnamp_batch_device,
+ * d_out is [npairs][5][(JJMAX+1)*NK*NK] complex (njkk, hjkk, nn, zz, j2). */
+int pnamp_project_device(pnamp_ctx *ctx, int npairs, const double *d_zres, int chop,
+                         double *d_out, void *stream);
+
+/* Synchronise the context's work; returns the first CUDA error seen. */
+int pnamp_sync(pnamp_ctx *ctx);
+
+/* Free the context and its device memory. */
+void pnamp_free(pnamp_ctx *ctx);
+
+/* Static text for a return code. */
+const char *pnamp_strerror(int code);
+
+/* Library version string. */
+const char *pnamp_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PNAMP_GPU_H */

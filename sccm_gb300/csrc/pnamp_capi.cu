@@ -1,0 +1,467 @@
+// C ABI of the PNAMP kernel library (declared in include/pnamp_gpu.h).
+//
+// Host side of Kernel4Triaxial: validates the caller's model space, Hamiltonian
+// and mesh, builds the small constant tables the kernels read (rotation block
+// map, Euler point list, sparse one-body operators, packed two-body list,
+// projection weights), plans where the per-point work arrays live (shared
+// memory when they fit a CTA, otherwise an L2-resident global slot per CTA),
+// and enqueues setup -> points -> projection on one stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "pnamp_gpu.h"
+#include "pnamp_internal.h"
+
+using namespace pnamp;
+
+struct pnamp_ctx {
+    Params p;
+    int core_prot, core_neut;
+    int axial;
+    int grid;
+    std::vector<void *> allocs;
+    double *d_pairbuf = nullptr;
+    long long pair_cap = 0;
+    zc *d_scratch = nullptr;
+    zc *d_projw = nullptr;
+    double *d_uv = nullptr, *d_zres = nullptr, *d_proj = nullptr;
+    int *d_status = nullptr;
+    long long batch_cap = 0;
+    cudaStream_t stream = nullptr;
+    int sticky = 0;
+};
+
+namespace {
+
+#define CK(call)                                                                  \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) {                                                  \
+            if (getenv("PNAMP_DEBUG"))                                            \
+                fprintf(stderr, "pnamp: %s:%d %s\n", __FILE__, __LINE__,          \
+                        cudaGetErrorString(e_));                                  \
+            return (e_ == cudaErrorMemoryAllocation) ? PNAMP_ERR_NOMEM : PNAMP_ERR_CUDA; \
+        }                                                                         \
+    } while (0)
+
+template <typename T>
+int dev_upload(pnamp_ctx *c, const std::vector<T> &h, const T **out) {
+    T *d = nullptr;
+    const size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
+    CK(cudaMalloc(&d, bytes));
+    c->allocs.push_back(d);
+    if (!h.empty()) CK(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *out = d;
+    return PNAMP_OK;
+}
+
+int plan_placement(Params &p, int smem_max) {
+    const int n = p.n, N = p.N2;
+    const long long nn = (long long)n * n;
+    Placement &pl = p.place;
+    auto align = [](int x) { return (x + 15) & ~15; };
+    // fixed shared pieces
+    int fixed = 0;
+    pl.off_piv = fixed; fixed += align((n + 8) * 4);
+    pl.off_inv = fixed; fixed += align(n * 16);
+    pl.off_red = fixed; fixed += align(40 * (kThreads / 32) * 8);
+    pl.off_rot = fixed; fixed += align(p.rot_elems * 16);
+    pl.off_vec = fixed; fixed += align((N + kNobs) * 16);
+    const int bs = (int)(4 * nn * 16), bt = (int)(nn * 16), by = (int)(2 * nn * 16), buv = (int)(2 * nn * 8);
+    // greedy: keep the hottest arrays in shared memory
+    int flags[4] = {1, 1, 1, 1};  // s, t, y, uv
+    const int order[4] = {3, 2, 1, 0};  // spill uv first, then y, t, s
+    auto total = [&]() { return fixed + flags[0] * bs + flags[1] * bt + flags[2] * by + flags[3] * buv; };
+    for (int k = 0; k < 4 && total() > smem_max; ++k) flags[order[k]] = 0;
+    if (total() > smem_max) return PNAMP_ERR_UNSUPPORTED;
+    int off = fixed;
+    pl.s_smem = flags[0]; pl.t_smem = flags[1]; pl.y_smem = flags[2]; pl.uv_smem = flags[3];
+    if (pl.s_smem) { pl.off_s = off; off += bs; }
+    if (pl.t_smem) { pl.off_t = off; off += bt; }
+    if (pl.y_smem) { pl.off_y = off; off += by; }
+    if (pl.uv_smem) { pl.off_uv = off; off += buv; }
+    pl.smem_bytes = off;
+    long long g = 0;
+    pl.g_x = g; g += nn;
+    pl.g_b = g; g += 2 * nn;
+    pl.g_p = g; g += 4 * nn;
+    pl.g_rw = g; g += nn;
+    pl.g_s = g; if (!pl.s_smem) g += 4 * nn;
+    pl.g_t = g; if (!pl.t_smem) g += nn;
+    pl.g_y = g; if (!pl.y_smem) g += 2 * nn;
+    pl.g_uv = g; if (!pl.uv_smem) g += nn;  // 2 n^2 doubles = n^2 complex slots
+    pl.slot_elems = (g + 15) & ~15LL;
+    return PNAMP_OK;
+}
+
+int ensure_pairs(pnamp_ctx *c, int npairs) {
+    if (npairs <= c->pair_cap) return PNAMP_OK;
+    if (c->d_pairbuf) cudaFree(c->d_pairbuf);
+    c->d_pairbuf = nullptr;
+    c->pair_cap = 0;
+    CK(cudaMalloc(&c->d_pairbuf, (size_t)npairs * c->p.pl.stride * sizeof(double)));
+    c->pair_cap = npairs;
+    return PNAMP_OK;
+}
+
+int ensure_batch(pnamp_ctx *c, int npairs) {
+    if (npairs <= c->batch_cap) return PNAMP_OK;
+    for (void *q : {(void *)c->d_uv, (void *)c->d_zres, (void *)c->d_status, (void *)c->d_proj})
+        if (q) cudaFree(q);
+    c->d_uv = c->d_zres = c->d_proj = nullptr;
+    c->d_status = nullptr;
+    c->batch_cap = 0;
+    const long long nn = (long long)c->p.n * c->p.n;
+    const long long fs = (long long)(kJJMax + 1) * kNK * kNK;
+    CK(cudaMalloc(&c->d_uv, (size_t)npairs * 4 * nn * sizeof(double)));
+    CK(cudaMalloc(&c->d_zres, (size_t)npairs * 2 * kNobs * c->p.n_euler * sizeof(double)));
+    CK(cudaMalloc(&c->d_status, (size_t)npairs * c->p.n_euler * sizeof(int)));
+    CK(cudaMalloc(&c->d_proj, (size_t)npairs * 2 * kProjFields * fs * sizeof(double)));
+    c->batch_cap = npairs;
+    return PNAMP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *pnamp_strerror(int code) {
+    switch (code) {
+        case PNAMP_OK: return "ok";
+        case PNAMP_ERR_ARG: return "invalid argument";
+        case PNAMP_ERR_CUDA: return "CUDA runtime error or no CUDA device";
+        case PNAMP_ERR_NOMEM: return "device allocation failed";
+        case PNAMP_ERR_SINGULAR_U: return "U of a vacuum is singular (zbareover/Pfaf_Over LU failure)";
+        case PNAMP_ERR_UNSUPPORTED: return "size not supported by this build";
+        case PNAMP_ERR_STATE: return "call order violated";
+        default: return "unknown error";
+    }
+}
+
+const char *pnamp_version(void) { return "sccm_gb300 pnamp 0.1 (sm_103a, fp64)"; }
+
+int pnamp_n_euler(const pnamp_ctx *ctx) { return ctx ? ctx->p.n_euler : -1; }
+
+void pnamp_free(pnamp_ctx *ctx) {
+    if (!ctx) return;
+    for (void *q : ctx->allocs) cudaFree(q);
+    for (void *q : {(void *)ctx->d_pairbuf, (void *)ctx->d_scratch, (void *)ctx->d_uv, (void *)ctx->d_zres,
+                    (void *)ctx->d_status, (void *)ctx->d_proj})
+        if (q) cudaFree(q);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_mesh *m, pnamp_ctx **out) {
+    if (!out) return PNAMP_ERR_ARG;
+    *out = nullptr;
+    if (!sp || !h || !m) return PNAMP_ERR_ARG;
+    const int n = sp->nlev;
+    if (n < 2 || n % 2 || !sp->t || !sp->n || !sp->l || !sp->twoj || !sp->twom) return PNAMP_ERR_ARG;
+    if (n > PNAMP_MAX_NLEV) return PNAMP_ERR_UNSUPPORTED;
+    if (sp->nprot < 0 || sp->nneut < 0) return PNAMP_ERR_ARG;
+    const int hh = n / 2;
+    // species halves and rotation blocks: runs of 2j+1 states of one (t,n,l,j), m = j..-j
+    std::vector<int> blk_start, blk_size, blk_tj, blk_roff, row_blk(n), twom(sp->twom, sp->twom + n);
+    int rot = 0;
+    for (int a = 0; a < n;) {
+        const int tj = sp->twoj[a];
+        if (tj < 1 || tj % 2 == 0 || tj > 15) return PNAMP_ERR_ARG;
+        if ((a < hh) != (sp->t[a] == -1)) return PNAMP_ERR_ARG;
+        const int d = tj + 1;
+        if (a + d > n) return PNAMP_ERR_ARG;
+        for (int i = 0; i < d; ++i) {
+            const int b = a + i;
+            if (sp->t[b] != sp->t[a] || sp->n[b] != sp->n[a] || sp->l[b] != sp->l[a] || sp->twoj[b] != tj ||
+                sp->twom[b] != tj - 2 * i)
+                return PNAMP_ERR_ARG;
+            row_blk[b] = (int)blk_start.size();
+        }
+        if ((int)blk_start.size() >= kMaxBlocks) return PNAMP_ERR_UNSUPPORTED;
+        blk_start.push_back(a);
+        blk_size.push_back(d);
+        blk_tj.push_back(tj);
+        blk_roff.push_back(rot);
+        rot += d * d;
+        a += d;
+    }
+    // mesh
+    if (m->nalp < 1 || m->nbet < 1 || m->ngam < 1 || m->nfom < 1) return PNAMP_ERR_ARG;
+    if (m->ncosbet != 1 && m->ncosbet != 2) return PNAMP_ERR_ARG;
+    if (!m->alpha || !m->beta || !m->gamma || !m->walp || !m->wbet || !m->wgam) return PNAMP_ERR_ARG;
+    const int nbu = std::max(m->nbet / m->ncosbet, 1);
+    std::vector<double> euler;
+    for (int k = 0; k < nbu; ++k)  // beta outer, alpha, gamma inner (Kernel3D.f90:200-217)
+        for (int ka = 0; ka < m->nalp; ++ka)
+            for (int kg = 0; kg < m->ngam; ++kg) {
+                euler.push_back(m->alpha[ka]);
+                euler.push_back(m->beta[k]);
+                euler.push_back(m->gamma[kg]);
+                euler.push_back(m->walp[ka] * m->wbet[k] * m->wgam[kg] * m->ncosbet);
+            }
+    // two-body list
+    if (h->nrec < 0 || (h->nrec > 0 && (!h->ka || !h->kb || !h->kc || !h->kd || !h->vbar))) return PNAMP_ERR_ARG;
+    if (!h->t1b) return PNAMP_ERR_ARG;
+    std::vector<uint32_t> rec_idx(h->nrec);
+    std::vector<double> rec_v(h->vbar, h->vbar + h->nrec);
+    for (int e = 0; e < h->nrec; ++e) {
+        const int a = h->ka[e] - 1, b = h->kb[e] - 1, c = h->kc[e] - 1, d = h->kd[e] - 1;
+        if (a < 0 || b < 0 || c < 0 || d < 0 || a >= n || b >= n || c >= n || d >= n) return PNAMP_ERR_ARG;
+        rec_idx[e] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c << 16) | ((uint32_t)d << 24);
+    }
+    // one-body tables
+    std::vector<int> t1b_idx;
+    std::vector<double> t1b_val;
+    for (int a = 0; a < n; ++a)
+        for (int c = 0; c < n; ++c) {  // sum_{a,c} rho(c,a) t(a,c)
+            const double v = h->t1b[a + (size_t)c * n];
+            if (v != 0.0) {
+                t1b_idx.push_back(c * n + a);
+                t1b_val.push_back(v);
+            }
+        }
+    std::vector<int> q_idx;
+    std::vector<double> q_val;
+    ObsTables ot{};
+    ot.q_off[0] = 0;
+    for (int q = 0; q < kNTrace; ++q) {
+        if (h->q2) {
+            const double *Q = h->q2 + (size_t)(q % 5) * n * n;
+            for (int a = 0; a < hh; ++a)
+                for (int b = 0; b < n; ++b) {
+                    // ZQ2: Q(a,b) rho(b,a); ZQ2t: Q(b,a) rho(b,a), proton rows a
+                    const double v = (q < 5) ? Q[a + (size_t)b * n] : Q[b + (size_t)a * n];
+                    if (v != 0.0) {
+                        q_idx.push_back(b * n + a);
+                        q_val.push_back(v);
+                    }
+                }
+        }
+        ot.q_off[q + 1] = (int)q_idx.size();
+    }
+    // J operators (zJiME, PNAMP_ME1B.f90:332-422): row and column sparsity, <= 2 per line
+    std::vector<int> jr_col(3 * 2 * n, -1), jc_row(3 * 2 * n, -1);
+    std::vector<zc> jr_val(3 * 2 * n, mk(0, 0)), jc_val(3 * 2 * n, mk(0, 0));
+    std::vector<double> jj1(n);
+    for (int a = 0; a < n; ++a) jj1[a] = 0.25 * sp->twoj[a] * (sp->twoj[a] + 2);
+    for (int a = 0; a < n; ++a)
+        for (int b = 0; b < n; ++b) {
+            if (sp->n[a] != sp->n[b] || sp->l[a] != sp->l[b] || sp->twoj[a] != sp->twoj[b] || sp->t[a] != sp->t[b])
+                continue;
+            const double jb = sp->twoj[b] / 2.0, mb = sp->twom[b] / 2.0;
+            const int ma2 = sp->twom[a], mb2 = sp->twom[b];
+            const double fp1 = jb * (jb + 1) - mb * (mb + 1), fm1 = jb * (jb + 1) - mb * (mb - 1);
+            zc vals[3] = {mk(0, 0), mk(0, 0), mk(0, 0)};
+            if (ma2 == mb2 + 2) {
+                vals[0] = mk(0.5 * std::sqrt(fp1), 0);
+                vals[1] = mk(0, -0.5 * std::sqrt(fp1));
+            } else if (ma2 == mb2 - 2) {
+                vals[0] = mk(0.5 * std::sqrt(fm1), 0);
+                vals[1] = mk(0, 0.5 * std::sqrt(fm1));
+            } else if (ma2 == mb2) {
+                vals[2] = mk(mb, 0);
+            }
+            for (int ax = 0; ax < 3; ++ax) {
+                if (vals[ax].x == 0.0 && vals[ax].y == 0.0) continue;
+                int *rc = &jr_col[(ax * n + a) * 2];
+                zc *rv = &jr_val[(ax * n + a) * 2];
+                const int sr = (rc[0] < 0) ? 0 : 1;
+                if (rc[sr] >= 0 && sr == 1) return PNAMP_ERR_ARG;
+                rc[sr] = b;
+                rv[sr] = vals[ax];
+                int *cr = &jc_row[(ax * n + b) * 2];
+                zc *cv = &jc_val[(ax * n + b) * 2];
+                const int sc = (cr[0] < 0) ? 0 : 1;
+                cr[sc] = a;
+                cv[sc] = vals[ax];
+            }
+        }
+
+    pnamp_ctx *c = new pnamp_ctx();
+    int dev = 0, rc = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        delete c;
+        return PNAMP_ERR_CUDA;
+    }
+    Params &p = c->p;
+    p.n = n;
+    p.h = hh;
+    p.N2 = 2 * n;
+    p.nprot = sp->nprot;
+    p.nneut = sp->nneut;
+    p.n_euler = (int)(euler.size() / 4);
+    p.nfom = m->nfom;
+    p.n_gauge = m->nfom * m->nfom;
+    p.cscale = m->cscale;
+    p.e0 = h->e0;
+    {
+        const long long aaa = (long long)n * (n + 1) / 2;
+        const double snpfaf = (aaa % 2) ? -1.0 : 1.0;
+        const int ex = n * m->iscale / 2;
+        p.vacfac = snpfaf * std::pow(10.0, -2.0 * ex);
+    }
+    p.iE2 = h->q2 ? 1 : 0;
+    p.nblk = (int)blk_start.size();
+    p.rot_elems = rot;
+    p.nrec = h->nrec;
+    p.pl.make(n);
+    c->core_prot = sp->core_prot;
+    c->core_neut = sp->core_neut;
+    c->axial = (m->nalp * m->ngam == 1) ? 1 : 0;
+    std::vector<double> fact(24);
+    fact[0] = 1.0;
+    for (int k = 1; k < 24; ++k) fact[k] = fact[k - 1] * k;
+#define UP(vec, dst)                                   \
+    if ((rc = dev_upload(c, vec, &(dst))) != PNAMP_OK) { \
+        pnamp_free(c);                                 \
+        return rc;                                     \
+    }
+    UP(blk_start, p.blk_start);
+    UP(blk_size, p.blk_size);
+    UP(blk_tj, p.blk_tj);
+    UP(blk_roff, p.blk_roff);
+    UP(row_blk, p.row_blk);
+    UP(twom, p.twom);
+    UP(euler, p.euler);
+    UP(fact, p.fact);
+    UP(rec_idx, p.rec_idx);
+    UP(rec_v, p.rec_v);
+    ot.n_t1b = (int)t1b_idx.size();
+    UP(t1b_idx, ot.t1b_idx);
+    UP(t1b_val, ot.t1b_val);
+    UP(q_idx, ot.q_idx);
+    UP(q_val, ot.q_val);
+    UP(jr_col, ot.jr_col);
+    UP(jr_val, ot.jr_val);
+    UP(jc_row, ot.jc_row);
+    UP(jc_val, ot.jc_val);
+    UP(jj1, ot.jj1);
+#undef UP
+    p.obs = ot;
+    int smem_optin = 0, nsm = 0;
+    if (cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        pnamp_free(c);
+        return PNAMP_ERR_CUDA;
+    }
+    if ((rc = plan_placement(p, smem_optin)) != PNAMP_OK) {
+        pnamp_free(c);
+        return rc;
+    }
+    if (set_point_smem(p.place.smem_bytes) != cudaSuccess) {
+        pnamp_free(c);
+        return PNAMP_ERR_CUDA;
+    }
+    int per_sm = 0;
+    if (point_blocks_per_sm(p.place.smem_bytes, &per_sm) != cudaSuccess || per_sm < 1) {
+        pnamp_free(c);
+        return PNAMP_ERR_CUDA;
+    }
+    c->grid = nsm * per_sm;
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        pnamp_free(c);
+        return PNAMP_ERR_CUDA;
+    }
+    if (cudaMalloc(&c->d_scratch, (size_t)c->grid * p.place.slot_elems * sizeof(zc)) != cudaSuccess) {
+        pnamp_free(c);
+        return PNAMP_ERR_NOMEM;
+    }
+    if (cudaMalloc(&c->d_projw, (size_t)p.n_euler * kNJKK * sizeof(zc)) != cudaSuccess) {
+        pnamp_free(c);
+        return PNAMP_ERR_NOMEM;
+    }
+    if (launch_proj_weights(p, c->axial, c->d_projw, c->stream) != cudaSuccess ||
+        cudaStreamSynchronize(c->stream) != cudaSuccess) {
+        pnamp_free(c);
+        return PNAMP_ERR_CUDA;
+    }
+    *out = c;
+    return PNAMP_OK;
+}
+
+int pnamp_batch_device(pnamp_ctx *c, int npairs, const double *d_uv, double *d_zres, int *d_status, void *stream) {
+    if (!c || npairs < 0 || (npairs > 0 && (!d_uv || !d_zres || !d_status))) return PNAMP_ERR_ARG;
+    if (npairs == 0) return PNAMP_OK;
+    int rc = ensure_pairs(c, npairs);
+    if (rc) return rc;
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    CK(launch_setup(c->p, npairs, d_uv, c->d_pairbuf, st));
+    CK(launch_points(c->p, npairs, c->d_pairbuf, c->d_scratch, c->grid, d_zres, d_status, st));
+    return PNAMP_OK;
+}
+
+int pnamp_batch(pnamp_ctx *c, int npairs, const double *uv, double *zres, int *point_status) {
+    if (!c || npairs < 0 || (npairs > 0 && (!uv || !zres))) return PNAMP_ERR_ARG;
+    if (npairs == 0) return PNAMP_OK;
+    int rc = ensure_batch(c, npairs);
+    if (rc) return rc;
+    const long long nn = (long long)c->p.n * c->p.n;
+    const size_t zbytes = (size_t)npairs * 2 * kNobs * c->p.n_euler * sizeof(double);
+    const size_t sbytes = (size_t)npairs * c->p.n_euler * sizeof(int);
+    CK(cudaMemcpyAsync(c->d_uv, uv, (size_t)npairs * 4 * nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    rc = pnamp_batch_device(c, npairs, c->d_uv, c->d_zres, c->d_status, c->stream);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(zres, c->d_zres, zbytes, cudaMemcpyDeviceToHost, c->stream));
+    std::vector<int> st((size_t)npairs * c->p.n_euler);
+    CK(cudaMemcpyAsync(st.data(), c->d_status, sbytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (point_status) memcpy(point_status, st.data(), sbytes);
+    for (int v : st)
+        if (v & PNAMP_ST_SINGULAR_U) return PNAMP_ERR_SINGULAR_U;
+    return PNAMP_OK;
+}
+
+int pnamp_pair(pnamp_ctx *c, const double *U0, const double *V0, const double *U1, const double *V1, double *zres,
+               int *point_status) {
+    if (!c || !U0 || !V0 || !U1 || !V1 || !zres) return PNAMP_ERR_ARG;
+    const size_t nn = (size_t)c->p.n * c->p.n;
+    std::vector<double> uv(4 * nn);
+    memcpy(uv.data(), U0, nn * sizeof(double));
+    memcpy(uv.data() + nn, V0, nn * sizeof(double));
+    memcpy(uv.data() + 2 * nn, U1, nn * sizeof(double));
+    memcpy(uv.data() + 3 * nn, V1, nn * sizeof(double));
+    return pnamp_batch(c, 1, uv.data(), zres, point_status);
+}
+
+int pnamp_project_device(pnamp_ctx *c, int npairs, const double *d_zres, int chop, double *d_out, void *stream) {
+    if (!c || npairs < 0 || (npairs > 0 && (!d_zres || !d_out))) return PNAMP_ERR_ARG;
+    if (npairs == 0) return PNAMP_OK;
+    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    const long long fs = (long long)(kJJMax + 1) * kNK * kNK;
+    CK(cudaMemsetAsync(d_out, 0, (size_t)npairs * 2 * kProjFields * fs * sizeof(double), st));
+    CK(launch_project(c->p, npairs, c->d_projw, d_zres, c->core_prot, c->core_neut, chop, d_out, st));
+    return PNAMP_OK;
+}
+
+int pnamp_project(pnamp_ctx *c, const double *zres, int chop, pnamp_kernels *out) {
+    if (!c || !zres || !out || !out->njkk || !out->hjkk || !out->nn || !out->zz || !out->j2) return PNAMP_ERR_ARG;
+    int rc = ensure_batch(c, 1);
+    if (rc) return rc;
+    const size_t zbytes = (size_t)2 * kNobs * c->p.n_euler * sizeof(double);
+    const size_t fs = (size_t)(kJJMax + 1) * kNK * kNK;
+    CK(cudaMemcpyAsync(c->d_zres, zres, zbytes, cudaMemcpyHostToDevice, c->stream));
+    rc = pnamp_project_device(c, 1, c->d_zres, chop, c->d_proj, c->stream);
+    if (rc) return rc;
+    std::vector<double> h(2 * kProjFields * fs);
+    CK(cudaMemcpyAsync(h.data(), c->d_proj, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    double *dst[kProjFields] = {out->njkk, out->hjkk, out->nn, out->zz, out->j2};
+    for (int q = 0; q < kProjFields; ++q) memcpy(dst[q], h.data() + 2 * q * fs, 2 * fs * sizeof(double));
+    return PNAMP_OK;
+}
+
+int pnamp_sync(pnamp_ctx *c) {
+    if (!c) return PNAMP_ERR_ARG;
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    return PNAMP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,93 @@
+// Internal interface between the C ABI (pnamp_capi.cu) and the kernels
+// (pnamp_kernels.cu). Not part of the public header.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "pnamp_device.cuh"
+
+namespace pnamp {
+
+constexpr int kNobs = 19;
+constexpr int kJJMax = 6;
+constexpr int kNK = 2 * kJJMax + 1;
+constexpr int kMaxN = 64;
+constexpr int kMaxBlocks = 64;           // rotation blocks (t, n, l, j) of a model space
+constexpr int kThreads = 256;            // threads per CTA of the point kernel
+constexpr int kNTrace = 10;              // proton traces of Q_{2mu} rho and Q_{2mu}^dagger rho
+constexpr int kNJKK = 1 + 25 + 81 + 169; // (J, K1, K2) with even J <= 6
+constexpr int kProjFields = 5;           // njkk, hjkk, nn, zz, j2
+constexpr int kSetupThreads = 256;
+
+// One pair record (doubles), all matrices row-major n x n:
+// U0 V0 U1 V1 W Z0 then [det0, det1, status-as-double, pad].
+struct PairLayout {
+    long long u0, v0, u1, v1, w, z0, dets, stride;
+    __host__ __device__ void make(int n) {
+        long long nn = (long long)n * n;
+        u0 = 0; v0 = nn; u1 = 2 * nn; v1 = 3 * nn; w = 4 * nn; z0 = 5 * nn; dets = 6 * nn;
+        stride = 6 * nn + 4;
+    }
+};
+
+// Where the per-point work arrays live: shared memory or the CTA's global slot.
+// Offsets are in bytes (shared) or complex elements (global slot).
+struct Placement {
+    int s_smem, t_smem, y_smem, uv_smem;
+    int off_s, off_t, off_y, off_uv;     // shared byte offsets (when *_smem)
+    int off_piv, off_inv, off_red, off_rot, off_vec;
+    int smem_bytes;
+    long long g_x, g_b, g_p, g_rw, g_s, g_t, g_y, g_uv;
+    long long slot_elems;
+};
+
+// Sparse one-body data used by the observables, built on the host once.
+struct ObsTables {
+    int n_t1b;                 // entries of the single-particle matrix
+    const int *t1b_idx;        // index into rho (c*n + a) for t(a,c) rho(c,a)
+    const double *t1b_val;
+    int q_off[kNTrace + 1];    // entry ranges per trace
+    const int *q_idx;          // index into rho
+    const double *q_val;
+    const int *jr_col;         // [3][n][2] row sparsity of Jx, Jy, Jz (column or -1)
+    const zc *jr_val;          // [3][n][2]
+    const int *jc_row;         // [3][n][2] column sparsity (row or -1)
+    const zc *jc_val;          // [3][n][2]
+    const double *jj1;         // [n] j(j+1)
+};
+
+struct Params {
+    int n, h, N2;              // n, n/2, 2n
+    int nprot, nneut;
+    int n_euler, nfom, n_gauge;
+    double cscale;
+    double e0;                 // H%E0, added to every energy (Kernel3D.f90:324)
+    double vacfac;             // (-1)^{n(n+1)/2} * 10^(-2*(n*iscale/2))
+    int iE2;
+    // rotation blocks
+    int nblk, rot_elems;
+    const int *blk_start, *blk_size, *blk_tj, *blk_roff, *row_blk, *twom;
+    const double *euler;       // [n_euler][4] alpha, beta, gamma, weight
+    const double *fact;        // k!, k = 0..23
+    // Hamiltonian two-body list
+    int nrec;
+    const uint32_t *rec_idx;   // packed 8-bit a,b,c,d (0-based)
+    const double *rec_v;
+    ObsTables obs;
+    PairLayout pl;
+    Placement place;
+};
+
+// launchers (pnamp_kernels.cu)
+cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *pairbuf,
+                         cudaStream_t st);
+cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc *scratch,
+                          int grid, double *zres, int *status, cudaStream_t st);
+cudaError_t launch_proj_weights(const Params &p, int axial, zc *w, cudaStream_t st);
+cudaError_t launch_project(const Params &p, int npairs, const zc *w, const double *zres,
+                           int core_prot, int core_neut, int chop, double *out, cudaStream_t st);
+cudaError_t set_point_smem(int bytes);
+cudaError_t point_blocks_per_sm(int smem_bytes, int *per_sm);
+int setup_smem_bytes(int n);
+
+}  // namespace pnamp

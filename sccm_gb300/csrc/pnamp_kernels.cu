@@ -1,0 +1,688 @@
+// PNAMP kernels for GB300 (sm_103a), FP64.
+//
+// Work decomposition (one CUDA launch per stage, batched over pairs):
+//   setup_kernel   one CTA per (q,q') pair: W = V1 U1^-1, Z0 = V0 U0^-1 and the
+//                  bare-vacuum overlaps det(1 + Z^T Z)^(-1/4)
+//                  (reference: zbareover, Codes/PNAMP/PNAMP_Proj.f90:6-79).
+//   point_kernel   persistent; one CTA per (pair, Euler point) work item at a
+//                  time. Per Euler point it builds the block-diagonal Wigner-D
+//                  rotation R (ROTATION_MAT, PNAMP_Proj.f90:83-136) and the
+//                  gauge-independent pieces X = R W R^T, R V1, R* U1 and the four
+//                  species partials of T22; then for each of the NFOM^2 gauge
+//                  points: the Pfaffian of Cscale [[D X D, -I], [I, -Z0]] with the
+//                  reference's pivoting and sign (Pfaf_Over + ZPfaffianF + ZExch,
+//                  PNAMP_Proj.f90:142-392), the LU of T22 and two row solves
+//                  giving rho, kappa10, kappa01 (ROKAPPAphiomega, :459-551), and
+//                  the observables of Kernel3D.f90:296-358 (ZN_0, the energy of
+//                  PNAMP_Energy_OpenMP.f90:31-90, ZJ2_0, ZQ2/ZQ2t), summed into
+//                  ZRES(iang, io) (Kernel3D.f90:385-387).
+//   project_kernel J/K projection of ZRES (Kernel3D.f90:415-751, plain form of
+//                  PNAMP_Kernel3D_v2.f90:477-498).
+//
+// Algebra used instead of the reference's per-point LU inverses (exact in
+// exact arithmetic): with A = D_phi R, D_phi = diag(e^{i phi_p}, e^{i phi_n}),
+//   conj(Vbar1) conj(Ubar1)^-1 = A V1 U1^-1 A^T = D (R W R^T) D,
+//   T22 = V0^T A V1 + U0^T A* U1 = sum_s e^{+-i phi_s} (species partials),
+//   rho = D (R V1 T22^-1) V0^T, kappa10 = D (R V1 T22^-1) U0^T,
+//   kappa01 = -D* (R* U1 T22^-1) V0^T.
+#include "pnamp_internal.h"
+
+namespace pnamp {
+
+// ------------------------------------------------------------------ scalars
+__device__ __forceinline__ double sabs1(double a) { return fabs(a); }
+__device__ __forceinline__ double sabs1(zc a) { return fabs(a.x) + fabs(a.y); }
+__device__ __forceinline__ double srecip(double a) { return 1.0 / a; }
+__device__ __forceinline__ zc srecip(zc a) { return zrecip(a); }
+__device__ __forceinline__ double smul(double a, double b) { return a * b; }
+__device__ __forceinline__ zc smul(zc a, zc b) { return a * b; }
+__device__ __forceinline__ double sfms(double a, double b, double c) { return fma(-a, b, c); }
+__device__ __forceinline__ zc sfms(zc a, zc b, zc c) { return zfms(a, b, c); }
+template <typename T> __device__ __forceinline__ T szero();
+template <> __device__ __forceinline__ double szero<double>() { return 0.0; }
+template <> __device__ __forceinline__ zc szero<zc>() { return mk(0.0, 0.0); }
+
+// Pivot row for column k (largest |re|+|im|, first on ties, as IZAMAX): warp 0
+// searches, the result is broadcast through sh[0] (row) and sh[1] (zero column).
+template <typename T>
+__device__ __forceinline__ int pivot_search(const T *A, int lda, int k, int n, int *sh, bool &zero) {
+    if (threadIdx.x < 32) {
+        double v = -1.0;
+        int idx = 0x7fffffff;
+        for (int i = k + (int)threadIdx.x; i < n; i += 32) {
+            const double a = sabs1(A[i * lda + k]);
+            if (a > v) {
+                v = a;
+                idx = i;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_down_sync(0xffffffffu, v, o);
+            const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+            if (ov > v || (ov == v && oi < idx)) {
+                v = ov;
+                idx = oi;
+            }
+        }
+        if (threadIdx.x == 0) {
+            // no comparable entry (all NaN): report a zero column, keep row k
+            const bool none = (idx == 0x7fffffff);
+            sh[0] = none ? k : idx;
+            sh[1] = (none || v == 0.0) ? 1 : 0;
+        }
+    }
+    __syncthreads();
+    zero = sh[1] != 0;
+    return sh[0];
+}
+
+// In-place LU with partial pivoting, P A = L U (L unit lower). perm[k] is the
+// row exchanged with row k at step k (LAPACK ipiv, 0-based); invd[k] = 1/U_kk.
+// Returns true if an exactly zero pivot column was met.
+template <typename T>
+__device__ bool lu_factor(T *A, int n, int lda, int *perm, T *invd, int *sh) {
+    bool sing = false;
+    for (int k = 0; k < n; ++k) {
+        bool zero;
+        const int p = pivot_search(A, lda, k, n, sh, zero);
+        if (p != k)
+            for (int j = threadIdx.x; j < n; j += blockDim.x) {
+                const T t = A[k * lda + j];
+                A[k * lda + j] = A[p * lda + j];
+                A[p * lda + j] = t;
+            }
+        if (threadIdx.x == 0) perm[k] = p;
+        __syncthreads();
+        if (zero) {
+            sing = true;
+            if (threadIdx.x == 0) invd[k] = szero<T>();
+            continue;
+        }
+        const T inv = srecip(A[k * lda + k]);
+        if (threadIdx.x == 0) invd[k] = inv;
+        for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[i * lda + k] = smul(A[i * lda + k], inv);
+        __syncthreads();
+        const int m = n - k - 1;
+        for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+            const int i = k + 1 + t / m, j = k + 1 + t % m;
+            A[i * lda + j] = sfms(A[i * lda + k], A[k * lda + j], A[i * lda + j]);
+        }
+        __syncthreads();
+    }
+    return sing;
+}
+
+// Y <- Y A^-1 for nr rows of Y (leading dimension ldy), A = P^T L U from lu_factor.
+template <typename T>
+__device__ void row_solve(T *Y, int nr, int ldy, const T *A, int n, int lda, const int *perm,
+                          const T *invd) {
+    for (int j = 0; j < n; ++j) {  // Z U = B, column by column
+        const T inv = invd[j];
+        for (int r = threadIdx.x; r < nr; r += blockDim.x) Y[r * ldy + j] = smul(Y[r * ldy + j], inv);
+        __syncthreads();
+        const int m = n - j - 1;
+        if (m > 0) {
+            for (int t = threadIdx.x; t < nr * m; t += blockDim.x) {
+                const int r = t / m, c = j + 1 + t % m;
+                Y[r * ldy + c] = sfms(Y[r * ldy + j], A[j * lda + c], Y[r * ldy + c]);
+            }
+            __syncthreads();
+        }
+    }
+    for (int j = n - 1; j > 0; --j) {  // Y2 L = Z, last column first
+        for (int t = threadIdx.x; t < nr * j; t += blockDim.x) {
+            const int r = t / j, c = t % j;
+            Y[r * ldy + c] = sfms(Y[r * ldy + j], A[j * lda + c], Y[r * ldy + c]);
+        }
+        __syncthreads();
+    }
+    for (int r = threadIdx.x; r < nr; r += blockDim.x)  // Y = Y2 P: column swaps in reverse
+        for (int k = n - 1; k >= 0; --k) {
+            const int p = perm[k];
+            if (p != k) {
+                const T t = Y[r * ldy + k];
+                Y[r * ldy + k] = Y[r * ldy + p];
+                Y[r * ldy + p] = t;
+            }
+        }
+    __syncthreads();
+}
+
+// ------------------------------------------------------------------ Pfaffian
+// Exchange of indices p < q of a skew matrix held in its upper triangle, rows
+// >= r only (ZExch, PNAMP_Proj.f90:356-392). Every thread touches distinct entries.
+__device__ __forceinline__ void exch_upper(zc *S, int N, int r, int p, int q) {
+    for (int i = r + threadIdx.x; i < N; i += blockDim.x) {
+        if (i < p) {
+            const zc t = S[i * N + p];
+            S[i * N + p] = S[i * N + q];
+            S[i * N + q] = t;
+        } else if (i > q) {
+            const zc t = S[p * N + i];
+            S[p * N + i] = S[q * N + i];
+            S[q * N + i] = t;
+        } else if (i > p && i < q) {
+            const zc t = S[p * N + i];
+            S[p * N + i] = -S[i * N + q];
+            S[i * N + q] = -t;
+        } else if (i == p) {
+            S[p * N + q] = -S[p * N + q];
+        }
+    }
+    __syncthreads();
+}
+
+// Pfaffian of the N x N skew matrix in the upper triangle of S (row-major),
+// ZPfaffianF (PNAMP_Proj.f90:218-350): at each 2x2 step the largest |S_ij| of
+// the remaining upper triangle (row-major scan, first maximum) is moved to
+// (r, r+1), the sign flips once per exchange, Pf = 0 when |pivot| <= 1e-13,
+// and the Schur complement is updated in place. `vec` holds N scratch values.
+__device__ zc pfaffian_upper(zc *S, int N, zc *vec, double *red, int &underflow) {
+    zc pf = mk(1.0, 0.0);
+    underflow = 0;
+    const int NB = N / 2;
+    for (int k = 0; k < NB - 1; ++k) {
+        const int r = 2 * k, c = r + 1, m = N - r;
+        const int T = m * (m - 1) / 2;
+        double best = -1.0;
+        int bidx = 0x7fffffff;
+        for (int t = threadIdx.x; t < T; t += blockDim.x) {
+            int i, j;
+            tri_index(t, m, i, j);
+            const double v = abs2(S[(r + i) * N + r + j]);
+            if (v > best) {
+                best = v;
+                bidx = t;
+            }
+        }
+        block_argmax(best, bidx, red);
+        if (bidx == 0x7fffffff) {  // only non-finite entries left: no pivot exists
+            underflow = 2;
+            return mk(0.0, 0.0);
+        }
+        int i1, i2;
+        tri_index(bidx, m, i1, i2);
+        i1 += r;
+        i2 += r;
+        double phas = 1.0;
+        if (i1 == r) phas = -phas;
+        if (i2 == c) phas = -phas;
+        if (i1 != r) exch_upper(S, N, r, r, i1);
+        if (i2 != c) exch_upper(S, N, r, c, i2);
+        const zc ss = S[r * N + c];
+        if (!(abs2(ss) > 1.0e-26)) {
+            underflow = 1;
+            __syncthreads();
+            return mk(0.0, 0.0);
+        }
+        const zc inv = zrecip(ss);
+        for (int i = c + 1 + threadIdx.x; i < N; i += blockDim.x) vec[i] = S[c * N + i] * inv;
+        __syncthreads();
+        const int mm = N - c - 1, TT = mm * (mm - 1) / 2;
+        for (int t = threadIdx.x; t < TT; t += blockDim.x) {
+            int i, j;
+            tri_index(t, mm, i, j);
+            i += c + 1;
+            j += c + 1;
+            zc s = S[i * N + j];
+            s = zfma(vec[i], S[r * N + j], s);
+            s = zfms(S[r * N + i], vec[j], s);
+            S[i * N + j] = s;
+        }
+        pf = phas * (pf * ss);
+        __syncthreads();
+    }
+    pf = pf * S[(N - 2) * N + N - 1];
+    __syncthreads();
+    return pf;
+}
+
+// ------------------------------------------------------------------ setup
+__global__ void __launch_bounds__(kSetupThreads)
+setup_kernel(Params p, const double *__restrict__ uv, double *__restrict__ pairbuf) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = p.n;
+    const long long nn = (long long)n * n;
+    const double *in = uv + (long long)blockIdx.x * 4 * nn;
+    double *out = pairbuf + (long long)blockIdx.x * p.pl.stride;
+    double *A = reinterpret_cast<double *>(smem_raw);
+    double *Yb = A + nn;
+    double *invd = Yb + nn;
+    double *red = invd + n;
+    int *perm = reinterpret_cast<int *>(red + 64);
+    int *sh = perm + n;
+    // column-major input -> row-major pair record (U0, V0, U1, V1)
+    for (long long t = threadIdx.x; t < 4 * nn; t += blockDim.x) {
+        const long long q = t / nn, e = t % nn;
+        const int i = (int)(e / n), j = (int)(e % n);
+        out[q * nn + e] = in[q * nn + i + (long long)j * n];
+    }
+    __syncthreads();
+    int st = 0;
+    for (int which = 0; which < 2; ++which) {
+        const double *U = out + (which == 0 ? p.pl.u1 : p.pl.u0);
+        const double *V = out + (which == 0 ? p.pl.v1 : p.pl.v0);
+        double *Z = out + (which == 0 ? p.pl.w : p.pl.z0);
+        for (long long t = threadIdx.x; t < nn; t += blockDim.x) {
+            A[t] = U[t];
+            Yb[t] = V[t];
+        }
+        __syncthreads();
+        if (lu_factor<double>(A, n, n, perm, invd, sh)) st = 1;
+        row_solve<double>(Yb, n, n, A, n, n, perm, invd);  // Z = V U^-1
+        for (long long t = threadIdx.x; t < nn; t += blockDim.x) Z[t] = Yb[t];
+        __syncthreads();
+        // det(1 + Z^T Z)^(-1/4): the eigenvalue product of zbareover, via LU
+        for (long long t = threadIdx.x; t < nn; t += blockDim.x) {
+            const int i = (int)(t / n), j = (int)(t % n);
+            double s = (i == j) ? 1.0 : 0.0;
+            for (int k = 0; k < n; ++k) s = fma(Yb[k * n + i], Yb[k * n + j], s);
+            A[t] = s;
+        }
+        __syncthreads();
+        if (lu_factor<double>(A, n, n, perm, invd, sh)) st = 1;
+        double v[1] = {0.0};
+        for (int k = threadIdx.x; k < n; k += blockDim.x) v[0] += log(fabs(A[k * n + k]));
+        block_sum<1>(v, red);
+        if (threadIdx.x == 0) out[p.pl.dets + (which == 0 ? 1 : 0)] = exp(-0.25 * v[0]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[p.pl.dets + 2] = (double)st;
+        out[p.pl.dets + 3] = 0.0;
+    }
+}
+
+int setup_smem_bytes(int n) { return (2 * n * n + n + 64) * 8 + (n + 8) * 4; }
+
+cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *pairbuf, cudaStream_t st) {
+    const int smem = setup_smem_bytes(p.n);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+    }
+    setup_kernel<<<npairs, kSetupThreads, smem, st>>>(p, uv, pairbuf);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ points
+constexpr int kNPart = 36;  // 18 complex partial sums per gauge point
+
+__global__ void __launch_bounds__(kThreads, 1)
+point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scratch,
+             double *__restrict__ zres, int *__restrict__ status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int n = p.n, h = p.h, N = p.N2;
+    const int nn = n * n;
+    const Placement &pl = p.place;
+    zc *slot = scratch + (long long)blockIdx.x * pl.slot_elems;
+    zc *X = slot + pl.g_x;    // R W R^T
+    zc *B = slot + pl.g_b;    // rows 0..n-1: R V1, rows n..2n-1: conj(R) U1
+    zc *P = slot + pl.g_p;    // T22 partials: V0p, V0n, U0p, U0n
+    zc *RW = slot + pl.g_rw;  // R W
+    zc *S = pl.s_smem ? reinterpret_cast<zc *>(smem + pl.off_s) : slot + pl.g_s;
+    zc *T = pl.t_smem ? reinterpret_cast<zc *>(smem + pl.off_t) : slot + pl.g_t;
+    zc *Y = pl.y_smem ? reinterpret_cast<zc *>(smem + pl.off_y) : slot + pl.g_y;
+    double *V0s = pl.uv_smem ? reinterpret_cast<double *>(smem + pl.off_uv)
+                             : reinterpret_cast<double *>(slot + pl.g_uv);
+    double *U0s = V0s + nn;
+    int *perm = reinterpret_cast<int *>(smem + pl.off_piv);
+    int *sh = perm + n;
+    zc *invd = reinterpret_cast<zc *>(smem + pl.off_inv);
+    double *red = reinterpret_cast<double *>(smem + pl.off_red);
+    zc *rot = reinterpret_cast<zc *>(smem + pl.off_rot);
+    zc *vec = reinterpret_cast<zc *>(smem + pl.off_vec);
+    zc *acc = vec + N;  // kNobs accumulators
+    zc *rho = S, *k10 = S + nn, *k01 = S + 2 * nn;
+
+    const long long total = (long long)npairs * p.n_euler;
+    const double twopi = 6.283185307179586476925287;
+    int cur_pair = -1;
+    for (long long item = blockIdx.x; item < total; item += gridDim.x) {
+        const int pair = (int)(item / p.n_euler), ie = (int)(item % p.n_euler);
+        const double *pr = pairbuf + (long long)pair * p.pl.stride;
+        const double *gU1 = pr + p.pl.u1, *gV1 = pr + p.pl.v1;
+        const double *gW = pr + p.pl.w, *gZ0 = pr + p.pl.z0;
+        const double det0 = pr[p.pl.dets], det1 = pr[p.pl.dets + 1];
+        const int pst = (int)pr[p.pl.dets + 2];
+        double *zout = zres + 2LL * (long long)pair * kNobs * p.n_euler;
+        if (pst) {
+            for (int io = threadIdx.x; io < kNobs; io += blockDim.x) {
+                zout[2LL * (io * p.n_euler + ie)] = 0.0;
+                zout[2LL * (io * p.n_euler + ie) + 1] = 0.0;
+            }
+            if (threadIdx.x == 0) status[(long long)pair * p.n_euler + ie] = 8;
+            continue;
+        }
+        if (pair != cur_pair) {
+            __syncthreads();
+            for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+                V0s[t] = pr[p.pl.v0 + t];
+                U0s[t] = pr[p.pl.u0 + t];
+            }
+            cur_pair = pair;
+        }
+        // ---- rotation blocks R_b(i,k) = e^{-i alp m_i} d^j_{m_i m_k}(bet) e^{-i gam m_k}
+        const double alp = p.euler[4 * ie], bet = p.euler[4 * ie + 1], gam = p.euler[4 * ie + 2];
+        double cb, sb;
+        sincos(0.5 * bet, &sb, &cb);
+        for (int b = 0; b < p.nblk; ++b) {
+            const int d = p.blk_size[b], tj = p.blk_tj[b], ro = p.blk_roff[b];
+            for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+                const int i = e / d, k = e % d;
+                const int mi = tj - 2 * i, mkk = tj - 2 * k;
+                const double dv = wigner_d(tj, mi, mkk, cb, sb, p.fact);
+                rot[ro + e] = dv * expi(-0.5 * (alp * mi + gam * mkk));
+            }
+        }
+        if (threadIdx.x == 0) {
+            for (int io = 0; io < kNobs; ++io) acc[io] = mk(0.0, 0.0);
+        }
+        __syncthreads();
+        // ---- R W, R V1, conj(R) U1
+        for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+            const int a = t / n, j = t % n;
+            const int b = p.row_blk[a], s0 = p.blk_start[b], d = p.blk_size[b];
+            const zc *Rr = rot + p.blk_roff[b] + (a - s0) * d;
+            zc rw = mk(0, 0), b1 = mk(0, 0), b2 = mk(0, 0);
+            for (int k = 0; k < d; ++k) {
+                const zc r = Rr[k];
+                rw = rfma(gW[(s0 + k) * n + j], r, rw);
+                b1 = rfma(gV1[(s0 + k) * n + j], r, b1);
+                b2 = rfma(gU1[(s0 + k) * n + j], zconj(r), b2);
+            }
+            RW[t] = rw;
+            B[t] = b1;
+            B[nn + t] = b2;
+        }
+        __syncthreads();
+        // ---- X = (R W) R^T and the T22 partials
+        for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+            const int a = t / n, c = t % n;
+            const int b = p.row_blk[c], s0 = p.blk_start[b], d = p.blk_size[b];
+            const zc *Rr = rot + p.blk_roff[b] + (c - s0) * d;
+            zc x = mk(0, 0);
+            for (int k = 0; k < d; ++k) x = zfma(RW[a * n + s0 + k], Rr[k], x);
+            X[t] = x;
+        }
+        for (int t = threadIdx.x; t < 4 * nn; t += blockDim.x) {
+            const int q = t / nn, e = t % nn, i = e / n, j = e % n;
+            const double *M = (q < 2) ? V0s : U0s;
+            const zc *Bq = (q < 2) ? B : B + nn;
+            const int k0 = (q & 1) ? h : 0;
+            zc s = mk(0, 0);
+            for (int k = k0; k < k0 + h; ++k) s = rfma(M[k * n + i], Bq[k * n + j], s);
+            P[t] = s;
+        }
+        __syncthreads();
+
+        int flags = 0;
+        for (int lp = 0; lp < p.nfom; ++lp) {
+            const double php = (p.nfom == 1) ? 0.0 : twopi * lp / p.nfom;
+            const zc ep = expi(php);
+            for (int ln = 0; ln < p.nfom; ++ln) {
+                const double phn = (p.nfom == 1) ? 0.0 : twopi * ln / p.nfom;
+                const zc en = expi(phn);
+                // ---- S = Cscale [[D X D, -I], [I, -Z0]] (upper triangle)
+                const double cs = p.cscale;
+                for (int t = threadIdx.x; t < N * (N - 1) / 2; t += blockDim.x) {
+                    int i, j;
+                    tri_index(t, N, i, j);
+                    zc v;
+                    if (j < n) {
+                        const zc dd = ((i < h) ? ep : en) * ((j < h) ? ep : en);
+                        v = cs * (X[i * n + j] * dd);
+                    } else if (i < n) {
+                        v = mk((j - n == i) ? -cs : 0.0, 0.0);
+                    } else {
+                        v = mk(-cs * gZ0[(i - n) * n + (j - n)], 0.0);
+                    }
+                    S[i * N + j] = v;
+                }
+                __syncthreads();
+                int under;
+                const zc pf = pfaffian_upper(S, N, vec, red, under);
+                // ---- T22(phi) and right-hand sides
+                const zc epc = zconj(ep), enc = zconj(en);
+                for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+                    zc s = ep * P[t];
+                    s = zfma(en, P[nn + t], s);
+                    s = zfma(epc, P[2 * nn + t], s);
+                    s = zfma(enc, P[3 * nn + t], s);
+                    T[t] = s;
+                }
+                for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) Y[t] = B[t];
+                __syncthreads();
+                const bool sing = lu_factor<zc>(T, n, n, perm, invd, sh);
+                row_solve<zc>(Y, 2 * n, n, T, n, n, perm, invd);
+                // ---- densities into the Pfaffian's storage
+                for (int t = threadIdx.x; t < 3 * nn; t += blockDim.x) {
+                    const int q = t / nn, e = t % nn, i = e / n, j = e % n;
+                    const zc *Yr = (q == 2) ? Y + (n + i) * n : Y + i * n;
+                    const double *M = (q == 1) ? U0s + j * n : V0s + j * n;
+                    zc s = mk(0, 0);
+                    for (int k = 0; k < n; ++k) s = rfma(M[k], Yr[k], s);
+                    const zc di = (i < h) ? ep : en;
+                    S[t] = (q == 2) ? -(zconj(di) * s) : di * s;
+                }
+                __syncthreads();
+                // ---- observables (18 complex partial sums)
+                double part[kNPart];
+#pragma unroll
+                for (int q = 0; q < kNPart; ++q) part[q] = 0.0;
+                for (int a = threadIdx.x; a < n; a += blockDim.x) {
+                    const zc d = rho[a * n + a];
+                    if (a < h) { part[0] += d.x; part[1] += d.y; }
+                    else { part[2] += d.x; part[3] += d.y; }
+                    part[8] = fma(p.obs.jj1[a], d.x, part[8]);
+                    part[9] = fma(p.obs.jj1[a], d.y, part[9]);
+                }
+                for (int e = threadIdx.x; e < p.obs.n_t1b; e += blockDim.x) {
+                    const zc r = rho[p.obs.t1b_idx[e]];
+                    part[4] = fma(p.obs.t1b_val[e], r.x, part[4]);
+                    part[5] = fma(p.obs.t1b_val[e], r.y, part[5]);
+                }
+                {   // two-body energy, exact regrouping of the 8-term sum of
+                    // PNAMP_Energy_OpenMP.f90:40-78:
+                    // V[rho_ki rho_lj - rho_li rho_kj + d(rho_ik rho_jl - rho_jk rho_il)]
+                    // + V/4 [K01_ij K10_kl + d K01_kl K10_ij],  K_xy = kappa_xy - kappa_yx
+                    zc e2 = mk(0, 0);
+                    for (int e = threadIdx.x; e < p.nrec; e += blockDim.x) {
+                        const uint32_t pk = p.rec_idx[e];
+                        const int i = pk & 0xff, j = (pk >> 8) & 0xff, k = (pk >> 16) & 0xff, l = pk >> 24;
+                        const double v = p.rec_v[e];
+                        zc t = rho[k * n + i] * rho[l * n + j];
+                        t = zfms(rho[l * n + i], rho[k * n + j], t);
+                        const zc K01ij = k01[i * n + j] - k01[j * n + i];
+                        const zc K10kl = k10[k * n + l] - k10[l * n + k];
+                        zc u = K01ij * K10kl;
+                        if (i + j != k + l) {
+                            t = zfma(rho[i * n + k], rho[j * n + l], t);
+                            t = zfms(rho[j * n + k], rho[i * n + l], t);
+                            const zc K01kl = k01[k * n + l] - k01[l * n + k];
+                            const zc K10ij = k10[i * n + j] - k10[j * n + i];
+                            u = zfma(K01kl, K10ij, u);
+                        }
+                        t = rfma(0.25, u, t);
+                        e2 = rfma(v, t, e2);
+                    }
+                    part[6] += e2.x;
+                    part[7] += e2.y;
+                }
+                // <J^2> (ZJ2_0, PNAMP_ME2B.f90:45-147): sum_axes Tr(J^2 rho) [above,
+                // via j(j+1)] + Tr(J rho)^2 - Tr(J rho J rho) + Tr(J k10 J^T k01^T)
+                for (int ax = 0; ax < 3; ++ax) {
+                    const int *jrc = p.obs.jr_col + ax * 2 * n;
+                    const zc *jrv = p.obs.jr_val + ax * 2 * n;
+                    const int *jcr = p.obs.jc_row + ax * 2 * n;
+                    const zc *jcv = p.obs.jc_val + ax * 2 * n;
+                    zc tr2 = mk(0, 0), rest = mk(0, 0);
+                    for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+                        const int a = t / n, c = t % n;
+                        zc mac = mk(0, 0), mca = mk(0, 0), jk = mk(0, 0), kj = mk(0, 0);
+#pragma unroll
+                        for (int q = 0; q < 2; ++q) {
+                            const int b1 = jrc[2 * a + q];
+                            if (b1 >= 0) {
+                                mac = zfma(jrv[2 * a + q], rho[b1 * n + c], mac);
+                                jk = zfma(jrv[2 * a + q], k10[b1 * n + c], jk);
+                            }
+                            const int b2 = jrc[2 * c + q];
+                            if (b2 >= 0) mca = zfma(jrv[2 * c + q], rho[b2 * n + a], mca);
+                            const int b3 = jcr[2 * c + q];
+                            if (b3 >= 0) kj = zfma(k01[a * n + b3], jcv[2 * c + q], kj);
+                        }
+                        rest = zfms(mac, mca, rest);
+                        rest = zfma(jk, kj, rest);
+                        if (c == a) tr2 = tr2 + mac;
+                    }
+                    part[10 + 2 * ax] += tr2.x;
+                    part[11 + 2 * ax] += tr2.y;
+                    part[8] += rest.x;
+                    part[9] += rest.y;
+                }
+                if (p.iE2) {
+#pragma unroll
+                    for (int q = 0; q < kNTrace; ++q) {
+                        double sr = 0.0, si = 0.0;
+                        for (int e = p.obs.q_off[q] + threadIdx.x; e < p.obs.q_off[q + 1]; e += blockDim.x) {
+                            const zc r = rho[p.obs.q_idx[e]];
+                            sr = fma(p.obs.q_val[e], r.x, sr);
+                            si = fma(p.obs.q_val[e], r.y, si);
+                        }
+                        part[16 + 2 * q] += sr;
+                        part[17 + 2 * q] += si;
+                    }
+                }
+                block_sum<kNPart>(part, red);
+                if (threadIdx.x == 0) {
+                    const zc zph = expi(-(php * p.nprot + phn * p.nneut));
+                    const zc norm = (p.vacfac * det0 * det1) * (pf * zph);
+                    const zc zp = mk(part[0], part[1]), zn = mk(part[2], part[3]);
+                    const zc ekin = mk(part[4], part[5]), e2 = mk(part[6], part[7]);
+                    const zc t2x = mk(part[10], part[11]), t2y = mk(part[12], part[13]),
+                             t2z = mk(part[14], part[15]);
+                    const zc j2 = mk(part[8], part[9]) + t2x * t2x + t2y * t2y + t2z * t2z;
+                    acc[0] = acc[0] + norm;
+                    int f = (under == 1) ? 1 : (under == 2 ? 4 : 0);
+                    if (sing) {
+                        f |= 2;
+                    } else {
+                        acc[1] = zfma(norm, zp, acc[1]);
+                        acc[2] = zfma(norm, zn, acc[2]);
+                        acc[3] = zfma(norm, ekin, acc[3]);
+                        acc[6] = zfma(norm, ekin + e2 + mk(p.e0, 0.0), acc[6]);
+                        acc[7] = zfma(norm, j2, acc[7]);
+                        if (p.iE2)
+                            for (int q = 0; q < 5; ++q) {
+                                acc[8 + q] = zfma(norm, mk(part[16 + 2 * q], part[17 + 2 * q]), acc[8 + q]);
+                                acc[13 + q] = zfma(norm, mk(part[26 + 2 * q], part[27 + 2 * q]), acc[13 + q]);
+                            }
+                    }
+                    flags |= f;
+                }
+            }
+        }
+        if (threadIdx.x == 0) {
+            const double inv = 1.0 / ((double)p.nfom * p.nfom);
+            int f = flags;
+            for (int io = 0; io < kNobs; ++io) {
+                const zc v = inv * acc[io];
+                if (!zfinite(v)) f |= 4;
+                zout[2LL * (io * p.n_euler + ie)] = v.x;
+                zout[2LL * (io * p.n_euler + ie) + 1] = v.y;
+            }
+            status[(long long)pair * p.n_euler + ie] = f;
+        }
+        __syncthreads();
+    }
+}
+
+cudaError_t point_blocks_per_sm(int smem_bytes, int *per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, point_kernel, kThreads, smem_bytes);
+}
+
+cudaError_t set_point_smem(int bytes) {
+    return cudaFuncSetAttribute(point_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc *scratch, int grid,
+                          double *zres, int *status, cudaStream_t st) {
+    point_kernel<<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ projection
+// Weights W[ie][jkk] = wJ * w_ie * e^{i K1 alp} d^J_{K1K2}(bet) e^{i K2 gam}, jkk over
+// (J = 0,2,4,6; K1 = -J..J; K2 = -J..J), wJ = (2J+1)/(8 pi^2) or (2J+1)/2 for an
+// N_alp N_gam = 1 mesh (Kernel3D.f90:78-81).
+__global__ void proj_weights_kernel(Params p, int axial, zc *w) {
+    const int ie = blockIdx.x;
+    const double alp = p.euler[4 * ie], bet = p.euler[4 * ie + 1], gam = p.euler[4 * ie + 2],
+                 wt = p.euler[4 * ie + 3];
+    double cb, sb;
+    sincos(0.5 * bet, &sb, &cb);
+    for (int jkk = threadIdx.x; jkk < kNJKK; jkk += blockDim.x) {
+        int J = 0, rem = jkk;
+        while (rem >= (2 * J + 1) * (2 * J + 1)) {
+            rem -= (2 * J + 1) * (2 * J + 1);
+            J += 2;
+        }
+        const int K1 = rem / (2 * J + 1) - J, K2 = rem % (2 * J + 1) - J;
+        const double wj = axial ? (2.0 * J + 1.0) / 2.0 : (2.0 * J + 1.0) / (8.0 * M_PI * M_PI);
+        const double d = wigner_d(2 * J, 2 * K1, 2 * K2, cb, sb, p.fact);
+        w[(long long)ie * kNJKK + jkk] = (wj * wt * d) * expi(K1 * alp + K2 * gam);
+    }
+}
+
+__global__ void project_kernel(Params p, const zc *__restrict__ w, const double *__restrict__ zres,
+                               int core_prot, int core_neut, int chop, double *__restrict__ out) {
+    const int pair = blockIdx.x;
+    const int jkk = blockIdx.y * blockDim.x + threadIdx.x;
+    if (jkk >= kNJKK) return;
+    const double *z = zres + 2LL * pair * kNobs * p.n_euler;
+    zc s[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) s[q] = mk(0, 0);
+    for (int ie = 0; ie < p.n_euler; ++ie) {
+        const zc wv = w[(long long)ie * kNJKK + jkk];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const zc zv = mk(z[2LL * (q * p.n_euler + ie)], z[2LL * (q * p.n_euler + ie) + 1]);
+            s[q] = zfma(wv, zv, s[q]);
+        }
+    }
+    int J = 0, rem = jkk;
+    while (rem >= (2 * J + 1) * (2 * J + 1)) {
+        rem -= (2 * J + 1) * (2 * J + 1);
+        J += 2;
+    }
+    const int K1 = rem / (2 * J + 1) - J, K2 = rem % (2 * J + 1) - J;
+    const long long fs = (long long)(kJJMax + 1) * kNK * kNK;
+    const long long o = ((long long)J * kNK + (K1 + kJJMax)) * kNK + (K2 + kJJMax);
+    double *op = out + 2LL * pair * kProjFields * fs;
+    if (chop && !(sqrt(abs2(s[0])) >= 1.0e-8)) return;  // fields stay 0 (Kernel3D.f90:732)
+    const zc inv0 = zrecip(s[0]);
+    const zc f[kProjFields] = {s[0], s[6], s[2] * inv0 + mk(core_neut, 0), s[1] * inv0 + mk(core_prot, 0),
+                               s[7] * inv0};
+#pragma unroll
+    for (int q = 0; q < kProjFields; ++q) {
+        op[2 * (q * fs + o)] = f[q].x;
+        op[2 * (q * fs + o) + 1] = f[q].y;
+    }
+}
+
+cudaError_t launch_project(const Params &p, int npairs, const zc *w, const double *zres, int core_prot,
+                           int core_neut, int chop, double *out, cudaStream_t st) {
+    dim3 grid(npairs, (kNJKK + 127) / 128);
+    project_kernel<<<grid, 128, 0, st>>>(p, w, zres, core_prot, core_neut, chop, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_proj_weights(const Params &p, int axial, zc *w, cudaStream_t st) {
+    proj_weights_kernel<<<p.n_euler, 128, 0, st>>>(p, axial, w);
+    return cudaGetLastError();
+}
+
+}  // namespace pnamp

@@ -1,0 +1,264 @@
+"""Python host for the PNAMP C ABI (include/pnamp_gpu.h), via ctypes.
+
+Mirrors the reference's per-pair operator, `Kernel4Triaxial(lpr, Nphi1, Nphi2,
+NLEV)` (Codes/PNAMP/PNAMP_Kernel3D.f90:1): the module-state inputs it reads
+(model space `tnljm`, Hamiltonian `H`, one-body operators `cME1B`, mesh `AMP`/
+`PNP`, `Input%Cscale/iscale`) become the context built once by `PnampContext`,
+and each call takes the pair's U0, V0, U1, V1 and returns ZRES and the
+projected `Kernel%` fields that `post_general` writes (PNAMP_IO.f90:39-96).
+
+Errors: a non-zero return code of the library raises `PnampError` carrying the
+code, where the reference `stop`s. There is no CPU fallback: if the compiled
+library is missing or no CUDA device is usable, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from .basis import JJMAX, NOBS, Mesh, ModelSpace
+
+PNAMP_OK = 0
+PNAMP_ERR_ARG = 1
+PNAMP_ERR_CUDA = 2
+PNAMP_ERR_NOMEM = 3
+PNAMP_ERR_SINGULAR_U = 4
+PNAMP_ERR_UNSUPPORTED = 5
+
+ST_PIVOT_UNDERFLOW = 1
+ST_SINGULAR_T22 = 2
+ST_NONFINITE = 4
+ST_SINGULAR_U = 8
+
+NK = 2 * JJMAX + 1
+FIELDS = ("njkk", "hjkk", "nn", "zz", "J2")
+
+_LIBPATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libpnamp_gb300.so")
+_lib = None
+
+# Every symbol the public header declares (tests check the library exports them).
+EXPORTS = ("pnamp_init", "pnamp_n_euler", "pnamp_pair", "pnamp_batch", "pnamp_batch_device",
+           "pnamp_project", "pnamp_project_device", "pnamp_sync", "pnamp_free",
+           "pnamp_strerror", "pnamp_version")
+
+
+class PnampError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        self.code = code
+        msg = load_library().pnamp_strerror(code).decode() if _lib is not None else str(code)
+        super().__init__(f"{where}: {msg} (code {code})")
+
+
+class _Space(C.Structure):
+    _fields_ = [("nlev", C.c_int), ("nprot", C.c_int), ("nneut", C.c_int),
+                ("core_prot", C.c_int), ("core_neut", C.c_int),
+                ("t", C.POINTER(C.c_int)), ("n", C.POINTER(C.c_int)), ("l", C.POINTER(C.c_int)),
+                ("twoj", C.POINTER(C.c_int)), ("twom", C.POINTER(C.c_int))]
+
+
+class _Ham(C.Structure):
+    _fields_ = [("e0", C.c_double), ("t1b", C.POINTER(C.c_double)), ("nrec", C.c_int),
+                ("ka", C.POINTER(C.c_int)), ("kb", C.POINTER(C.c_int)),
+                ("kc", C.POINTER(C.c_int)), ("kd", C.POINTER(C.c_int)),
+                ("vbar", C.POINTER(C.c_double)), ("q2", C.POINTER(C.c_double))]
+
+
+class _Mesh(C.Structure):
+    _fields_ = [("nalp", C.c_int), ("nbet", C.c_int), ("ngam", C.c_int), ("nfom", C.c_int),
+                ("ncosbet", C.c_int),
+                ("alpha", C.POINTER(C.c_double)), ("walp", C.POINTER(C.c_double)),
+                ("beta", C.POINTER(C.c_double)), ("wbet", C.POINTER(C.c_double)),
+                ("gamma", C.POINTER(C.c_double)), ("wgam", C.POINTER(C.c_double)),
+                ("cscale", C.c_double), ("iscale", C.c_int)]
+
+
+class _Kernels(C.Structure):
+    _fields_ = [(f, C.POINTER(C.c_double)) for f in ("njkk", "hjkk", "nn", "zz", "j2")]
+
+
+def load_library(path: str | None = None):
+    """Load the compiled library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or _LIBPATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"PNAMP CUDA library not built ({p}); run sccm_gb300.build.build()")
+    lib = C.CDLL(p)
+    vp = C.c_void_p
+    lib.pnamp_init.argtypes = [C.POINTER(_Space), C.POINTER(_Ham), C.POINTER(_Mesh), C.POINTER(vp)]
+    lib.pnamp_n_euler.argtypes = [vp]
+    lib.pnamp_pair.argtypes = [vp] + [C.POINTER(C.c_double)] * 5 + [C.POINTER(C.c_int)]
+    lib.pnamp_batch.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                C.POINTER(C.c_int)]
+    lib.pnamp_batch_device.argtypes = [vp, C.c_int, vp, vp, vp, vp]
+    lib.pnamp_project.argtypes = [vp, C.POINTER(C.c_double), C.c_int, C.POINTER(_Kernels)]
+    lib.pnamp_project_device.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp]
+    lib.pnamp_sync.argtypes = [vp]
+    lib.pnamp_free.argtypes = [vp]
+    lib.pnamp_free.restype = None
+    lib.pnamp_strerror.argtypes = [C.c_int]
+    lib.pnamp_strerror.restype = C.c_char_p
+    lib.pnamp_version.restype = C.c_char_p
+    _lib = lib
+    return lib
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+@dataclass
+class PairResult:
+    zres: np.ndarray      # [P_E, NOBS] complex, ZRES(iang, io)
+    status: np.ndarray    # [P_E] int bit flags
+
+
+class PnampContext:
+    """A built PNAMP context: model space + Hamiltonian + mesh on the GPU."""
+
+    def __init__(self, sp: ModelSpace, e0: float, t1b, recs, vbar, mesh: Mesh,
+                 q2=None, cscale: float = 1.0, iscale: int = 0):
+        lib = load_library()
+        n = sp.nlev
+        self.sp, self.mesh, self.n = sp, mesh, n
+        keep = []
+
+        def ia(x):
+            a = np.ascontiguousarray(np.asarray(x, dtype=np.int32))
+            keep.append(a)
+            return a
+
+        def da(x):
+            a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+            keep.append(a)
+            return a
+
+        self._space = _Space(n, sp.nprot, sp.nneut, sp.core_prot, sp.core_neut,
+                             _iptr(ia(sp.t)), _iptr(ia(sp.n)), _iptr(ia(sp.l)),
+                             _iptr(ia(sp.twoj)), _iptr(ia(sp.twom)))
+        recs = np.asarray(recs, dtype=np.int32).reshape(-1, 4)
+        t1 = da(np.real(np.asarray(t1b)).T)        # column-major
+        q = None
+        if q2 is not None:
+            q = da(np.asarray(q2, dtype=np.float64).transpose(0, 2, 1))   # each block column-major
+        self._ham = _Ham(float(e0), _dptr(t1), int(recs.shape[0]),
+                         _iptr(ia(recs[:, 0] + 1)), _iptr(ia(recs[:, 1] + 1)),
+                         _iptr(ia(recs[:, 2] + 1)), _iptr(ia(recs[:, 3] + 1)),
+                         _dptr(da(vbar)), _dptr(q) if q is not None else None)
+        self._mesh = _Mesh(mesh.nalp, mesh.nbet, mesh.ngam, mesh.nfom, mesh.ncosbet,
+                           _dptr(da(mesh.alpha)), _dptr(da(mesh.walp)),
+                           _dptr(da(mesh.beta)), _dptr(da(mesh.wbet)),
+                           _dptr(da(mesh.gamma)), _dptr(da(mesh.wgam)),
+                           float(cscale), int(iscale))
+        self._keep = keep
+        h = C.c_void_p()
+        rc = lib.pnamp_init(C.byref(self._space), C.byref(self._ham), C.byref(self._mesh), C.byref(h))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_init")
+        self._h = h
+        self.n_euler = lib.pnamp_n_euler(h)
+
+    # ------------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().pnamp_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # ------------------------------------------------------------------
+    @staticmethod
+    def pack_pairs(pairs):
+        """[(U0, V0, U1, V1), ...] -> float64 [npairs, 4, n, n] in the ABI's column-major order."""
+        out = np.empty((len(pairs), 4) + np.shape(pairs[0][0]), dtype=np.float64)
+        for k, quad in enumerate(pairs):
+            for q in range(4):
+                out[k, q] = np.asarray(quad[q], dtype=np.float64).T
+        return out
+
+    def batch(self, pairs_or_packed, check=True):
+        """Mesh loop for a batch of pairs -> (zres [npairs, P_E, NOBS], status [npairs, P_E])."""
+        uv = pairs_or_packed if isinstance(pairs_or_packed, np.ndarray) else self.pack_pairs(pairs_or_packed)
+        uv = np.ascontiguousarray(uv, dtype=np.float64)
+        npairs = uv.shape[0]
+        z = np.zeros((npairs, NOBS, self.n_euler), dtype=np.complex128)
+        st = np.zeros((npairs, self.n_euler), dtype=np.int32)
+        rc = load_library().pnamp_batch(self._h, npairs, _dptr(uv),
+                                        z.ctypes.data_as(C.POINTER(C.c_double)), _iptr(st))
+        if rc != PNAMP_OK and (check or rc != PNAMP_ERR_SINGULAR_U):
+            raise PnampError(rc, "pnamp_batch")
+        return np.ascontiguousarray(z.transpose(0, 2, 1)), st
+
+    def pair(self, U0, V0, U1, V1) -> PairResult:
+        """One pair through `pnamp_pair` (host buffers)."""
+        n = self.n
+        bufs = [np.asfortranarray(np.asarray(x, dtype=np.float64)) for x in (U0, V0, U1, V1)]
+        for b in bufs:
+            if b.shape != (n, n):
+                raise ValueError(f"expected {n}x{n} matrices")
+        z = np.zeros((NOBS, self.n_euler), dtype=np.complex128)
+        st = np.zeros(self.n_euler, dtype=np.int32)
+        rc = load_library().pnamp_pair(self._h, *[_dptr(b) for b in bufs],
+                                       z.ctypes.data_as(C.POINTER(C.c_double)), _iptr(st))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_pair")
+        return PairResult(np.ascontiguousarray(z.T), st)
+
+    def project(self, zres, chop=True):
+        """J/K projection of one pair's ZRES [P_E, NOBS] -> dict field -> [J, K1+6, K2+6]."""
+        z = np.ascontiguousarray(np.asarray(zres, dtype=np.complex128).T)   # [NOBS, P_E]
+        if z.shape != (NOBS, self.n_euler):
+            raise ValueError("zres must be [P_E, NOBS]")
+        out = {f: np.zeros((JJMAX + 1, NK, NK), dtype=np.complex128) for f in FIELDS}
+        k = _Kernels(*[out[f].ctypes.data_as(C.POINTER(C.c_double)) for f in FIELDS])
+        rc = load_library().pnamp_project(self._h, z.ctypes.data_as(C.POINTER(C.c_double)),
+                                          1 if chop else 0, C.byref(k))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_project")
+        return out
+
+    # device-pointer entry points (inputs already resident in HBM)
+    def batch_device(self, npairs, d_uv, d_zres, d_status, stream=0):
+        rc = load_library().pnamp_batch_device(self._h, npairs, C.c_void_p(d_uv), C.c_void_p(d_zres),
+                                               C.c_void_p(d_status), C.c_void_p(stream))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_batch_device")
+
+    def project_device(self, npairs, d_zres, d_out, chop=True, stream=0):
+        rc = load_library().pnamp_project_device(self._h, npairs, C.c_void_p(d_zres), 1 if chop else 0,
+                                                 C.c_void_p(d_out), C.c_void_p(stream))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_project_device")
+
+    def sync(self):
+        rc = load_library().pnamp_sync(self._h)
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_sync")
+
+
+def kernel4triaxial(ctx: PnampContext, U0, V0, U1, V1, chop=True):
+    """Per-pair operator with the reference's name: ZRES and the projected Kernel fields."""
+    r = ctx.pair(U0, V0, U1, V1)
+    return r.zres, ctx.project(r.zres, chop=chop), r.status

@@ -1,0 +1,135 @@
+"""GPU (C-ABI) vs oracle parity on seeded inputs, and the Ge76 kernel files through the GPU.
+
+Tolerances (FP64 throughout):
+  * norm kernel N(Omega) = ZRES(:,1): 1e-10 relative to max |N| over the mesh
+  * the other observables ZRES(:,2..18): 1e-9 relative to max |column|
+  * projected fields vs the reference's Ge76 kernel files: 2e-7 relative
+    (the files print 8 significant digits)
+"""
+import numpy as np
+import pytest
+
+from sccm_gb300.basis import JJMAX, Mesh
+from sccm_gb300.pnamp import PnampContext, PnampError, PNAMP_ERR_SINGULAR_U
+from sccm_gb300.synth import make_workload
+from oracle.pnamp_oracle import Hamiltonian, kernel_triaxial, project
+
+pytestmark = pytest.mark.gpu
+
+NORM_TOL = 1e-10
+OBS_TOL = 1e-9
+
+
+def ctx_for(w, mesh, iE2=True):
+    return PnampContext(w.sp, w.e0, w.t1b, w.recs, w.vbar, mesh, q2=w.q2 if iE2 else None)
+
+
+def oracle_zres(w, mesh, i, j, iE2=True):
+    ham = Hamiltonian(w.e0, w.t1b, w.recs, w.vbar, w.q2, w.jops)
+    (U0, V0), (U1, V1) = w.vacua[i], w.vacua[j]
+    return kernel_triaxial(w.sp, ham, mesh, U0, V0, U1, V1, iE2=iE2)
+
+
+def assert_zres_close(z_gpu, z_ref):
+    nref = np.abs(z_ref[:, 0]).max()
+    err = np.abs(z_gpu[:, 0] - z_ref[:, 0]).max() / nref
+    assert err <= NORM_TOL, f"norm kernel rel err {err:.2e}"
+    for io in range(1, z_ref.shape[1]):
+        scale = np.abs(z_ref[:, io]).max()
+        if scale == 0.0:
+            assert np.abs(z_gpu[:, io]).max() == 0.0, io
+            continue
+        e = np.abs(z_gpu[:, io] - z_ref[:, io]).max() / scale
+        assert e <= OBS_TOL, f"observable {io + 1}: rel err {e:.2e}"
+
+
+@pytest.fixture(scope="module")
+def sd():
+    return make_workload("sd", 2, Mesh(3, 4, 3, 3), seed=101, deformed=False)
+
+
+@pytest.fixture(scope="module")
+def pf():
+    return make_workload("pf", 2, Mesh(2, 3, 2, 3), seed=202)
+
+
+def test_sd_pair_matches_oracle(sd):
+    with ctx_for(sd, sd.mesh) as ctx:
+        r = ctx.pair(*sd.vacua[0], *sd.vacua[1])
+    assert (r.status & ~1).max() == 0
+    assert_zres_close(r.zres, oracle_zres(sd, sd.mesh, 0, 1))
+
+
+def test_sd_diagonal_pair_matches_oracle(sd):
+    with ctx_for(sd, sd.mesh) as ctx:
+        z, st = ctx.batch([(*sd.vacua[1], *sd.vacua[1])])
+    assert_zres_close(z[0], oracle_zres(sd, sd.mesh, 1, 1))
+
+
+def test_pf_pair_matches_oracle(pf):
+    with ctx_for(pf, pf.mesh) as ctx:
+        r = ctx.pair(*pf.vacua[0], *pf.vacua[1])
+    assert_zres_close(r.zres, oracle_zres(pf, pf.mesh, 0, 1))
+
+
+def test_sdpf_n64_global_workspace_matches_oracle():
+    w = make_workload("sdpf", 2, Mesh(1, 2, 1, 2), seed=303)
+    with ctx_for(w, w.mesh) as ctx:
+        r = ctx.pair(*w.vacua[0], *w.vacua[1])
+    assert_zres_close(r.zres, oracle_zres(w, w.mesh, 0, 1))
+
+
+def test_norm_is_one_at_identity(sd):
+    mesh = Mesh(1, 1, 1, 1)
+    with ctx_for(sd, mesh) as ctx:
+        r = ctx.pair(*sd.vacua[0], *sd.vacua[0])
+    assert abs(r.zres[0, 0] - 1.0) < 1e-12
+    assert abs(r.zres[0, 1] - sd.sp.nprot) < 1e-10 and abs(r.zres[0, 2] - sd.sp.nneut) < 1e-10
+
+
+def test_batch_equals_single_pairs(sd):
+    with ctx_for(sd, sd.mesh) as ctx:
+        z, _ = ctx.batch([(*sd.vacua[0], *sd.vacua[1]), (*sd.vacua[1], *sd.vacua[0])])
+        a = ctx.pair(*sd.vacua[0], *sd.vacua[1]).zres
+        b = ctx.pair(*sd.vacua[1], *sd.vacua[0]).zres
+    assert np.array_equal(z[0], a) and np.array_equal(z[1], b)
+
+
+def test_projection_matches_oracle(sd):
+    z = oracle_zres(sd, sd.mesh, 0, 1)
+    ref = project(z, sd.mesh, chop=1e-8)
+    with ctx_for(sd, sd.mesh) as ctx:
+        got = ctx.project(z, chop=True)
+    for f in ("njkk", "hjkk", "nn", "zz", "J2"):
+        scale = max(np.abs(ref[f]).max(), 1e-30)
+        assert np.abs(got[f] - ref[f]).max() <= 1e-12 * scale + 1e-14, f
+
+
+def test_singular_u_is_reported(sd):
+    U, V = sd.vacua[0]
+    Us = U.copy()
+    Us[:, 3] = 0.0
+    with ctx_for(sd, Mesh(1, 1, 1, 1)) as ctx:
+        with pytest.raises(PnampError) as e:
+            ctx.pair(Us, V, U, V)
+    assert e.value.code == PNAMP_ERR_SINGULAR_U
+
+
+def test_ge76_kernel_files_through_gpu(ge76):
+    """All 16 intact Ge76 pairs in one batch reproduce the reference's kernel files."""
+    g = ge76
+    mesh = Mesh(1, g["nbet"], 1, g["nfom"], ncosbet=g["ncosbet"])
+    idx = [(i, j) for i in range(4) for j in range(4)]
+    with PnampContext(g["sp"], g["e0"], g["t1b"], g["recs"], g["vbar"], mesh, q2=g["q2"]) as ctx:
+        z, st = ctx.batch([(g["U"][i], g["V"][i], g["U"][j], g["V"][j]) for i, j in idx])
+        for k, (i, j) in enumerate(idx):
+            kern = ctx.project(z[k], chop=False)
+            gold = g["gold"][i, j]
+            n0 = abs(gold[0, 0])
+            for jj, J in enumerate(g["jvals"]):
+                if abs(gold[jj, 0]) < 1e-6 * n0:
+                    continue
+                for f, name in enumerate(("njkk", "hjkk", "nn", "zz", "J2")):
+                    mine = kern[name][J, JJMAX, JJMAX].real
+                    ref = gold[jj, f].real
+                    assert abs(mine - ref) <= 2e-7 * abs(ref) + 1e-12, ((i, j), J, name, mine, ref)
