@@ -1,0 +1,344 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 PNAMP kernel path: projected kernel points/s.
+
+Workload (the configuration the metric is quoted on that fits one GPU):
+pf shell (0f7/2, 1p3/2, 0f5/2, 1p1/2; n = 40 m-states), 4 + 4 valence
+nucleons, 20 seeded quadrupole-deformed HFB vacua (beta2 in [0, 0.5], gamma in
+[0, 60] deg) giving 210 symmetric (q, q') pairs, Euler mesh 10 x 20 x 10 with
+9 x 9 gauge points (162,000 kernel points per pair), seeded random J-coupled
+isospin-symmetric TBMEs. A kernel point is one (q, q', alpha, beta, gamma,
+phi_n, phi_p) evaluation. One step = `--pairs-per-step` pairs through the full
+per-pair path (setup, mesh loop, J/K projection); steps walk round robin over
+the pair list. For N > 1 (torchrun), pairs are dealt to ranks as in the
+reference's MPI round robin (rank == ic mod nprocs): weak scaling, no
+collective on the data path.
+
+`value`: device-resident inputs (uploaded before timing), CUDA-event time of
+the steps on the launching stream, L2 flushed (256 MiB write) before each step
+outside its events.  `e2e`: the same steps through the host-buffer C ABI
+(`pnamp_batch` + `pnamp_project`) from pinned host memory, results read back.
+`--impl reference`: the CPU oracle port (the reference Fortran cannot be
+compiled here), all host cores, bounded samples of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "projected kernel points/s on 1 GB300: learned+mixed vs plain FP64 at <=1 keV E_J"
+WORKLOAD = ("pf shell n=40 (Z=4, N=4 valence), 20 seeded deformed vacua -> 210 pairs, "
+            "Euler 10x20x10 x gauge 9x9 = 162000 points/pair, plain FP64 form")
+# Algorithmic FP64 work per kernel point (pf, n = 40, P_G = 81): rotation,
+# W-solve and T22 partials amortised over the gauge points plus the Pfaffian,
+# T22 inverse and density products: (8+24+16) n^3 / P_G + (10.7+16+40) n^3,
+# plus the irreducible sparse two-body contraction, 14,442 records x 24 flops.
+def algorithmic_flops_per_point(n, n_gauge, nrec):
+    return (48.0 * n ** 3 / n_gauge + (32.0 / 3.0 + 16.0 + 40.0) * n ** 3) + 24.0 * nrec
+
+
+SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+# ------------------------------------------------------------------ CPU oracle
+def _oracle_task(args):
+    sp, ham, mesh, U0, V0, U1, V1, ie = args
+    from oracle.pnamp_oracle import kernel_triaxial
+    z = kernel_triaxial(sp, ham, mesh, U0, V0, U1, V1, euler_subset=[ie])
+    return z[ie]
+
+
+def cpu_sample(pool, ncores, wl, n_euler_sample, pair_index=0):
+    """Oracle port on `n_euler_sample` Euler points x all gauge points of one pair."""
+    from oracle.pnamp_oracle import Hamiltonian
+    ham = Hamiltonian(wl.e0, wl.t1b, wl.recs, wl.vbar, wl.q2, wl.jops)
+    i, j = wl.pairs[pair_index]
+    (U0, V0), (U1, V1) = wl.vacua[i], wl.vacua[j]
+    P = wl.mesh.n_euler
+    tasks = [(wl.sp, ham, wl.mesh, U0, V0, U1, V1, (k * 7919) % P) for k in range(n_euler_sample)]
+    t0 = time.perf_counter()
+    pool.map(_oracle_task, tasks, chunksize=1)
+    dt = time.perf_counter() - t0
+    return n_euler_sample * wl.mesh.n_gauge / dt, dt
+
+
+def make_pool(ncores):
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    return mp.get_context("spawn").Pool(ncores)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={SMI_FIELDS}", "--format=csv",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self, device_index=0):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for ln in open(self.path).read().splitlines()[1:]:
+            tok = [t.strip() for t in ln.split(",")]
+            if len(tok) < 9 or not tok[0].isdigit() or int(tok[0]) != device_index:
+                continue
+            try:
+                rows.append((float(tok[1].split()[0]), float(tok[2].split()[0]), tok[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for _, _, fl in rows for k in range(4) if fl[k].lower() == "active"})
+        mx = max(r[1] for r in rows)
+        loaded = [r[0] for r in rows if r[0] > 0.3 * mx] or [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ main
+def fp64_peak_tflops(torch):
+    """cuBLAS DGEMM 4096^3, best of 5, CUDA events: the FP64 pipe ceiling on this GPU."""
+    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        a @ b
+    best = 1e30
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        a @ b
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e) / 1e3)
+    return 2 * 4096 ** 3 / best / 1e12
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--pairs-per-step", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--mesh", default=None,
+                    help="override the mesh as NALP,NBET,NGAM,NFOM (small cases for profiling captures)")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    ncores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+
+    from sccm_gb300.basis import Mesh
+    from sccm_gb300.synth import config
+    wl = config(1)
+    if args.mesh:
+        wl.mesh = Mesh(*[int(x) for x in args.mesh.split(",")])
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        pool = make_pool(ncores)
+        # bounded sample per step: ~ncores Euler points x all gauge points of pair 0
+        rate, dt = cpu_sample(pool, ncores, wl, ncores)          # calibration / warm-up
+        nsamp = max(ncores, int(ncores * max(1.0, 8.0 / max(dt, 1e-3))))
+        for _ in range(max(0, args.warmup - 1)):
+            cpu_sample(pool, ncores, wl, nsamp)
+        tot_pts, tot_t = 0, 0.0
+        for _ in range(args.steps):
+            r, t = cpu_sample(pool, ncores, wl, nsamp)
+            tot_pts += r * t
+            tot_t += t
+        pool.close()
+        v = tot_pts / tot_t
+        sample = f"{nsamp} Euler points x 81 gauge points of pair (0,0) per step"
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": v, "unit": "points/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD},
+            "cpu_baseline": {"value": v, "unit": "points/s", "cores": ncores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return 0
+
+    # CPU baseline pool before any GPU call (spawned workers never touch CUDA)
+    pool = None
+    if not args.no_cpu_baseline and rank == 0 and world == 1:
+        pool = make_pool(ncores)
+
+    import numpy as np
+    import torch
+    from sccm_gb300.driver import rank_pairs
+    from sccm_gb300.pnamp import PnampContext
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    ctx = PnampContext(wl.sp, wl.e0, wl.t1b, wl.recs, wl.vbar, wl.mesh, q2=wl.q2)
+    P = ctx.n_euler
+    G = wl.mesh.n_gauge
+    pts_per_pair = P * G
+    mine = rank_pairs(wl.pairs, rank, world)
+    pps = args.pairs_per_step
+    nsteps_total = args.warmup + args.steps
+    order = [mine[(k) % len(mine)] for k in range(nsteps_total * pps)]
+    quads = [(*wl.vacua[i], *wl.vacua[j]) for (i, j) in order]
+    packed = PnampContext.pack_pairs(quads)                           # [npairs, 4, n, n]
+    stream = torch.cuda.Stream()
+    dev = torch.device("cuda", local_rank)
+    fs = 5 * 7 * 13 * 13 * 2
+    with torch.cuda.stream(stream):
+        d_uv = torch.from_numpy(packed).to(dev)
+        d_z = torch.zeros((pps, 19 * P * 2), dtype=torch.float64, device=dev)
+        d_st = torch.zeros((pps, P), dtype=torch.int32, device=dev)
+        d_proj = torch.zeros((pps, fs), dtype=torch.float64, device=dev)
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    sh = stream.cuda_stream
+    per_pair_uv = packed[0].nbytes
+
+    def step(k, ev=None):
+        off = d_uv.data_ptr() + k * pps * per_pair_uv
+        if ev:
+            ev[0].record(stream)
+        ctx.batch_device(pps, off, d_z.data_ptr(), d_st.data_ptr(), sh)
+        if ev:
+            ev[1].record(stream)
+        ctx.project_device(pps, d_z.data_ptr(), d_proj.data_ptr(), True, sh)
+        if ev:
+            ev[2].record(stream)
+
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup):
+            flush.zero_()
+            step(k)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+        with ClockSampler(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv")
+                          if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else f"/tmp/pnamp_clocks_{rank}.csv") as clk:
+            torch.cuda.synchronize()
+            for k in range(args.steps):
+                flush.zero_()
+                step(args.warmup + k, evs[k])
+            torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    step_ms = [e[0].elapsed_time(e[2]) for e in evs]
+    kern_ms = [e[0].elapsed_time(e[1]) for e in evs]
+    total_s = sum(step_ms) / 1e3
+    if dist:
+        t = torch.tensor([total_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_s = float(t)
+    status = d_st.cpu().numpy()
+    if (status & ~1).any():
+        raise RuntimeError(f"non-trivial point status flags: {np.unique(status)}")
+    points = args.steps * pps * pts_per_pair * world
+    value = points / total_s
+    clocks = clk.summary(local_rank)
+
+    # ---- e2e through the host-buffer C ABI, pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        pin = torch.empty(packed.shape, dtype=torch.float64).pin_memory().numpy()
+        pin[...] = packed
+        h2d = pps * per_pair_uv + pps * 19 * P * 16
+        d2h = pps * 19 * P * 16 + pps * P * 4 + pps * fs * 8
+        for k in range(min(args.warmup, 1)):
+            ctx.batch(pin[k * pps:(k + 1) * pps])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            z, st = ctx.batch(pin[(args.warmup + k) * pps:(args.warmup + k + 1) * pps])
+            for q in range(pps):
+                ctx.project(z[q])
+        torch.cuda.synchronize()
+        te = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([te], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            te = float(t)
+        e2e = {"value": points / te, "unit": "points/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+
+    # ---- roofline of the dominant kernel (the point kernel; setup is < 0.1 %)
+    flops_pt = algorithmic_flops_per_point(wl.sp.nlev, G, len(wl.recs))
+    launch_s = statistics.mean(kern_ms) / 1e3
+    achieved = flops_pt * pps * pts_per_pair / launch_s / 1e12
+    peak = fp64_peak_tflops(torch) if rank == 0 else None
+
+    cpu = None
+    if pool is not None:
+        _, dt = cpu_sample(pool, ncores, wl, ncores)
+        nsamp = max(ncores, int(ncores * max(1.0, args.cpu_seconds / max(dt, 1e-3))))
+        rate, dt = cpu_sample(pool, ncores, wl, nsamp)
+        pool.close()
+        cpu = {"value": rate, "unit": "points/s", "cores": ncores, "kind": "port",
+               "sample": f"{nsamp} Euler points x 81 gauge points of pair (0,0), {dt:.1f} s, "
+                         f"oracle/pnamp_oracle.py on a spawn pool of {ncores} processes"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic: seeded vacua and TBMEs (no public dataset exists)",
+            "config": {"workload": WORKLOAD, "form": "plain FP64", "pairs_per_step": pps,
+                       "points_per_pair": pts_per_pair, "l2": "flushed (256 MiB write) before each step",
+                       "parallelism": f"pairs round-robin over {world} rank(s)"},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (achieved / peak) if peak else None, "traffic": None,
+                         "kernel": "point_kernel", "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                         "flops_per_point": flops_pt},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "clocks": clocks,
+            "gpu_launches": 3 * args.steps,
+        }
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -391,7 +391,7 @@ int pnamp_batch_device(pnamp_ctx *c, int npairs, const double *d_uv, double *d_z
     if (npairs == 0) return PNAMP_OK;
     int rc = ensure_pairs(c, npairs);
     if (rc) return rc;
-    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
     CK(launch_setup(c->p, npairs, d_uv, c->d_pairbuf, st));
     CK(launch_points(c->p, npairs, c->d_pairbuf, c->d_scratch, c->grid, d_zres, d_status, st));
     return PNAMP_OK;
@@ -433,7 +433,7 @@ int pnamp_pair(pnamp_ctx *c, const double *U0, const double *V0, const double *U
 int pnamp_project_device(pnamp_ctx *c, int npairs, const double *d_zres, int chop, double *d_out, void *stream) {
     if (!c || npairs < 0 || (npairs > 0 && (!d_zres || !d_out))) return PNAMP_ERR_ARG;
     if (npairs == 0) return PNAMP_OK;
-    cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
     const long long fs = (long long)(kJJMax + 1) * kNK * kNK;
     CK(cudaMemsetAsync(d_out, 0, (size_t)npairs * 2 * kProjFields * fs * sizeof(double), st));
     CK(launch_project(c->p, npairs, c->d_projw, d_zres, c->core_prot, c->core_neut, chop, d_out, st));

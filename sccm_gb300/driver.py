@@ -1,0 +1,70 @@
+"""Pair scheduling and kernel-file output: the host side of PNAMP_Main.
+
+  * `pair_list`: the (q, q') list of Codes/PNAMP/PNAMP_Main.f90:60-73
+    (ICons = 1: every q' in nq1i..nq1f; otherwise only q' >= q).
+  * `rank_pairs`: the static round robin of PNAMP_Main.f90:79-84,
+    `rank == mod(ic, nprocs)` with ic counted from 1. Pairs are independent,
+    so ranks need no collective: each writes its own kernel files.
+  * `run_pairs`: batches a rank's pairs through the GPU library, projects
+    them and writes `kern.*.elem` files through a temporary name and rename
+    (the kernel file is the checkpoint: a finished pair is never redone);
+    a manifest lists finished pairs so an interrupted run resumes.
+"""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+
+from .formats import atomic_write_text, write_elem_general
+from .pnamp import PnampContext
+
+
+def pair_list(nq0i, nq0f, nq1i, nq1f, icons=1):
+    out = []
+    for q1 in range(nq0i, nq0f + 1):
+        start = nq1i if icons == 1 else q1
+        for q2 in range(start, nq1f + 1):
+            out.append((q1, q2))
+    return out
+
+
+def rank_pairs(pairs, rank, nprocs):
+    """Pairs of this rank: ic = 1, 2, ... with rank == ic mod nprocs."""
+    return [p for ic, p in enumerate(pairs, start=1) if ic % nprocs == rank]
+
+
+def elem_name(prefix, q1, q2):
+    return f"{prefix}_{q1:03d}_{q2:03d}.elem"
+
+
+def run_pairs(ctx: PnampContext, vacua, pairs, out_dir, prefix="kern", coords=None, batch=8,
+              manifest="manifest.json"):
+    """Compute and write the kernel files of `pairs` ((q1, q2) 1-based into `vacua`)."""
+    os.makedirs(out_dir, exist_ok=True)
+    mpath = os.path.join(out_dir, manifest)
+    done = set()
+    if os.path.exists(mpath):
+        with open(mpath) as f:
+            done = {tuple(x) for x in json.load(f).get("done", [])}
+    todo = [p for p in pairs if tuple(p) not in done]
+    for s in range(0, len(todo), batch):
+        chunk = todo[s:s + batch]
+        quads = [(*vacua[q1 - 1], *vacua[q2 - 1]) for (q1, q2) in chunk]
+        zres, status = ctx.batch(quads)
+        for k, (q1, q2) in enumerate(chunk):
+            kern = ctx.project(zres[k], chop=True)
+            c1 = coords[q1 - 1] if coords is not None else (0.0, 0.0)
+            c2 = coords[q2 - 1] if coords is not None else (0.0, 0.0)
+            zero = np.zeros((7, 13, 13, 3), complex)
+            full = dict(kern, q0p=np.zeros((7, 13, 13), complex), q0pc=np.zeros((7, 13, 13), complex),
+                        qpred=zero, qcpred=zero)
+            atomic_write_text(os.path.join(out_dir, elem_name(prefix, q1, q2)), write_elem_general,
+                              full, c1, c2)
+            done.add((q1, q2))
+        tmp = mpath + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump({"done": sorted(done)}, f)
+        os.replace(tmp, mpath)
+    return sorted(done)
