@@ -44,6 +44,10 @@ extern "C" {
 #define PNAMP_ERR_SINGULAR_U 4   /* U of a vacuum is singular: zbareover/Pfaf_Over ZGETRF info != 0 */
 #define PNAMP_ERR_UNSUPPORTED 5  /* a size beyond what this build supports */
 #define PNAMP_ERR_STATE 6        /* call order violated */
+#define PNAMP_ERR_SCRATCH_LIMIT 7 /* request does not fit the fixed scratch of pnamp_batch_device_noalloc */
+
+/* Size of the fixed device scratch array used by pnamp_batch_device_noalloc. */
+#define PNAMP_NOALLOC_SCRATCH_BYTES (32u << 20)
 
 /* per-Euler-point status bits (OR over the gauge points of that Euler point) */
 #define PNAMP_ST_PIVOT_UNDERFLOW 1  /* Pfaffian pivot |ss| <= 1e-13: norm set to 0 (PNAMP_Proj.f90:290,333) */
@@ -120,6 +124,26 @@ int pnamp_batch(pnamp_ctx *ctx, int npairs, const double *uv, double *zres, int 
  * cudaStream_t, NULL = legacy default stream); returns after the launch. */
 int pnamp_batch_device(pnamp_ctx *ctx, int npairs, const double *d_uv,
                        double *d_zres, int *d_point_status, void *stream);
+
+/* Same computation as pnamp_batch_device, for callers that must not allocate
+ * device memory per call: code running under a runtime that owns the device
+ * memory budget (a caching allocator or an MPS client with a hard memory cap),
+ * or code that must not risk the implicit device synchronisation of
+ * cudaMalloc/cudaFree between stream-ordered steps. It calls no cudaMalloc,
+ * cudaFree or allocating library routine: the per-pair records and the per-CTA
+ * workspace live in one file-scope device array of PNAMP_NOALLOC_SCRATCH_BYTES
+ * (32 MiB), which every GPU that loads the library holds until exit. The context
+ * itself is still created once by pnamp_init. A request whose pair records plus
+ * one CTA workspace exceed the array is rejected with PNAMP_ERR_SCRATCH_LIMIT;
+ * otherwise the grid shrinks to the CTA workspaces that fit. The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) and caches
+ * it; make that first call before any stream capture. All calls share the array
+ * and it keeps the last call's contents; the kernels write every scratch byte
+ * before reading it, so nothing is cleared. Calls whose work overlaps on the GPU
+ * (different streams, or different host threads) race on the array: serialise
+ * them. This entry point has no counterpart in the reference. */
+int pnamp_batch_device_noalloc(pnamp_ctx *ctx, int npairs, const double *d_uv,
+                               double *d_zres, int *d_point_status, void *stream);
 
 /* J/K projection of one pair's ZRES into kernel-file fields (Kernel3D.f90:415-751,
  * plain D-function form of PNAMP_Kernel3D_v2.f90:477-498; for an N_alp*N_gam = 1

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "pnamp_gpu.h"
@@ -141,6 +142,8 @@ const char *pnamp_strerror(int code) {
         case PNAMP_ERR_SINGULAR_U: return "U of a vacuum is singular (zbareover/Pfaf_Over LU failure)";
         case PNAMP_ERR_UNSUPPORTED: return "size not supported by this build";
         case PNAMP_ERR_STATE: return "call order violated";
+        case PNAMP_ERR_SCRATCH_LIMIT:
+            return "request exceeds the fixed no-allocation scratch (PNAMP_NOALLOC_SCRATCH_BYTES)";
         default: return "unknown error";
     }
 }
@@ -465,3 +468,56 @@ int pnamp_sync(pnamp_ctx *c) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// No-allocation variant of pnamp_batch_device. The scratch it needs (pair
+// records from setup_kernel, per-CTA workspace slots of point_kernel) lives in
+// this file-scope array instead of context buffers from cudaMalloc. In host
+// code `g_noalloc_scratch` names a host-side stand-in, not a device address, so
+// the device address is looked up once per device with cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[PNAMP_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device (first call per
+// device resolves and caches it).
+int noalloc_scratch(void **out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return PNAMP_ERR_CUDA;
+    if (dev < 0 || dev >= kMaxDevices) return PNAMP_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) return PNAMP_ERR_CUDA;
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return PNAMP_OK;
+}
+}  // namespace
+
+extern "C" int pnamp_batch_device_noalloc(pnamp_ctx *c, int npairs, const double *d_uv, double *d_zres,
+                                          int *d_status, void *stream) {
+    if (!c || npairs < 0 || (npairs > 0 && (!d_uv || !d_zres || !d_status))) return PNAMP_ERR_ARG;
+    if (npairs == 0) return PNAMP_OK;
+    const unsigned long long cap = PNAMP_NOALLOC_SCRATCH_BYTES;
+    const unsigned long long pair_bytes =
+        ((unsigned long long)npairs * (unsigned long long)c->p.pl.stride * sizeof(double) + 255ull) & ~255ull;
+    const unsigned long long slot_bytes = (unsigned long long)c->p.place.slot_elems * sizeof(zc);
+    if (pair_bytes + slot_bytes > cap) return PNAMP_ERR_SCRATCH_LIMIT;
+    const unsigned long long fit = (cap - pair_bytes) / slot_bytes;
+    const int grid = (int)std::min<unsigned long long>((unsigned long long)c->grid, fit);
+    void *base = nullptr;
+    const int rc = noalloc_scratch(&base);
+    if (rc) return rc;
+    double *pairbuf = reinterpret_cast<double *>(base);
+    zc *slots = reinterpret_cast<zc *>(reinterpret_cast<unsigned char *>(base) + pair_bytes);
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
+    CK(launch_setup(c->p, npairs, d_uv, pairbuf, st));
+    CK(launch_points(c->p, npairs, pairbuf, slots, grid, d_zres, d_status, st));
+    return PNAMP_OK;
+}

@@ -42,7 +42,8 @@ _lib = None
 # Every symbol the public header declares (tests check the library exports them).
 EXPORTS = ("pnamp_init", "pnamp_n_euler", "pnamp_pair", "pnamp_batch", "pnamp_batch_device",
            "pnamp_project", "pnamp_project_device", "pnamp_sync", "pnamp_free",
-           "pnamp_strerror", "pnamp_version")
+           "pnamp_strerror", "pnamp_version", "pnamp_batch_device_noalloc")
+PNAMP_ERR_SCRATCH_LIMIT = 7
 
 
 class PnampError(RuntimeError):
@@ -95,6 +96,7 @@ def load_library(path: str | None = None):
     lib.pnamp_batch.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_int)]
     lib.pnamp_batch_device.argtypes = [vp, C.c_int, vp, vp, vp, vp]
+    lib.pnamp_batch_device_noalloc.argtypes = [vp, C.c_int, vp, vp, vp, vp]
     lib.pnamp_project.argtypes = [vp, C.POINTER(C.c_double), C.c_int, C.POINTER(_Kernels)]
     lib.pnamp_project_device.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp]
     lib.pnamp_sync.argtypes = [vp]
