@@ -249,43 +249,17 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
         }
         ot.q_off[q + 1] = (int)q_idx.size();
     }
-    // J operators (zJiME, PNAMP_ME1B.f90:332-422): row and column sparsity, <= 2 per line
-    std::vector<int> jr_col(3 * 2 * n, -1), jc_row(3 * 2 * n, -1);
-    std::vector<zc> jr_val(3 * 2 * n, mk(0, 0)), jc_val(3 * 2 * n, mk(0, 0));
-    std::vector<double> jj1(n);
-    for (int a = 0; a < n; ++a) jj1[a] = 0.25 * sp->twoj[a] * (sp->twoj[a] + 2);
-    for (int a = 0; a < n; ++a)
-        for (int b = 0; b < n; ++b) {
-            if (sp->n[a] != sp->n[b] || sp->l[a] != sp->l[b] || sp->twoj[a] != sp->twoj[b] || sp->t[a] != sp->t[b])
-                continue;
-            const double jb = sp->twoj[b] / 2.0, mb = sp->twom[b] / 2.0;
-            const int ma2 = sp->twom[a], mb2 = sp->twom[b];
-            const double fp1 = jb * (jb + 1) - mb * (mb + 1), fm1 = jb * (jb + 1) - mb * (mb - 1);
-            zc vals[3] = {mk(0, 0), mk(0, 0), mk(0, 0)};
-            if (ma2 == mb2 + 2) {
-                vals[0] = mk(0.5 * std::sqrt(fp1), 0);
-                vals[1] = mk(0, -0.5 * std::sqrt(fp1));
-            } else if (ma2 == mb2 - 2) {
-                vals[0] = mk(0.5 * std::sqrt(fm1), 0);
-                vals[1] = mk(0, 0.5 * std::sqrt(fm1));
-            } else if (ma2 == mb2) {
-                vals[2] = mk(mb, 0);
-            }
-            for (int ax = 0; ax < 3; ++ax) {
-                if (vals[ax].x == 0.0 && vals[ax].y == 0.0) continue;
-                int *rc = &jr_col[(ax * n + a) * 2];
-                zc *rv = &jr_val[(ax * n + a) * 2];
-                const int sr = (rc[0] < 0) ? 0 : 1;
-                if (rc[sr] >= 0 && sr == 1) return PNAMP_ERR_ARG;
-                rc[sr] = b;
-                rv[sr] = vals[ax];
-                int *cr = &jc_row[(ax * n + b) * 2];
-                zc *cv = &jc_val[(ax * n + b) * 2];
-                const int sc = (cr[0] < 0) ? 0 : 1;
-                cr[sc] = a;
-                cv[sc] = vals[ax];
-            }
-        }
+    // J operators (zJiME, PNAMP_ME1B.f90:332-422) as ladder coefficients: within a
+    // block m decreases by 1 from one state to the next, so J+ (m -> m+1) links
+    // a+1 -> a and J- links a-1 -> a.
+    std::vector<double> jpv(n, 0.0), jmv(n, 0.0), mzv(n), jj1(n);
+    for (int a = 0; a < n; ++a) {
+        const double j = sp->twoj[a] / 2.0, mm = sp->twom[a] / 2.0;
+        jj1[a] = j * (j + 1.0);
+        mzv[a] = mm;
+        if (a + 1 < n && row_blk[a + 1] == row_blk[a]) jpv[a] = std::sqrt(j * (j + 1.0) - (mm - 1.0) * mm);
+        if (a >= 1 && row_blk[a - 1] == row_blk[a]) jmv[a] = std::sqrt(j * (j + 1.0) - (mm + 1.0) * mm);
+    }
 
     pnamp_ctx *c = new pnamp_ctx();
     int dev = 0, rc = 0;
@@ -341,10 +315,9 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
     UP(t1b_val, ot.t1b_val);
     UP(q_idx, ot.q_idx);
     UP(q_val, ot.q_val);
-    UP(jr_col, ot.jr_col);
-    UP(jr_val, ot.jr_val);
-    UP(jc_row, ot.jc_row);
-    UP(jc_val, ot.jc_val);
+    UP(jpv, ot.jp);
+    UP(jmv, ot.jm);
+    UP(mzv, ot.mz);
     UP(jj1, ot.jj1);
 #undef UP
     p.obs = ot;

@@ -108,6 +108,51 @@ __device__ __forceinline__ void block_argmax(double &v, int &idx, double *buf) {
     __syncthreads();
 }
 
+// Max of a 64-bit key; ties broken towards the smallest idx. Broadcast to all.
+__device__ __forceinline__ void block_argmax_u64(unsigned long long &v, int &idx, double *buf) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    auto better = [](unsigned long long ov, int oi, unsigned long long v0, int i0) {
+        return oi != 0x7fffffff && (i0 == 0x7fffffff || ov > v0 || (ov == v0 && oi < i0));
+    };
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long ov = __shfl_down_sync(0xffffffffu, v, o);
+        const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+        if (better(ov, oi, v, idx)) {
+            v = ov;
+            idx = oi;
+        }
+    }
+    unsigned long long *kbuf = reinterpret_cast<unsigned long long *>(buf);
+    int *ibuf = reinterpret_cast<int *>(buf + nw);
+    if (lane == 0) {
+        kbuf[wid] = v;
+        ibuf[wid] = idx;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        v = lane < nw ? kbuf[lane] : 0ull;
+        idx = lane < nw ? ibuf[lane] : 0x7fffffff;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ov = __shfl_down_sync(0xffffffffu, v, o);
+            const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+            if (better(ov, oi, v, idx)) {
+                v = ov;
+                idx = oi;
+            }
+        }
+        if (lane == 0) {
+            kbuf[0] = v;
+            ibuf[0] = idx;
+        }
+    }
+    __syncthreads();
+    v = kbuf[0];
+    idx = ibuf[0];
+    __syncthreads();
+}
+
 // Sum NV doubles across the block; result valid in all threads.
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double *buf) {

@@ -49,10 +49,9 @@ struct ObsTables {
     int q_off[kNTrace + 1];    // entry ranges per trace
     const int *q_idx;          // index into rho
     const double *q_val;
-    const int *jr_col;         // [3][n][2] row sparsity of Jx, Jy, Jz (column or -1)
-    const zc *jr_val;          // [3][n][2]
-    const int *jc_row;         // [3][n][2] column sparsity (row or -1)
-    const zc *jc_val;          // [3][n][2]
+    const double *jp;          // [n] J+_{a,a+1} (0 at the last state of a block)
+    const double *jm;          // [n] J-_{a,a-1} (0 at the first state of a block)
+    const double *mz;          // [n] m_a
     const double *jj1;         // [n] j(j+1)
 };
 

@@ -185,19 +185,24 @@ __device__ zc pfaffian_upper(zc *S, int N, zc *vec, double *red, int &underflow)
     for (int k = 0; k < NB - 1; ++k) {
         const int r = 2 * k, c = r + 1, m = N - r;
         const int T = m * (m - 1) / 2;
-        double best = -1.0;
+        // pivot key: max(|re|, |im|) compared as the integer bit patterns of
+        // non-negative doubles (exact order, no FP64 instructions)
+        unsigned long long best = 0ull;
         int bidx = 0x7fffffff;
         for (int t = threadIdx.x; t < T; t += blockDim.x) {
             int i, j;
             tri_index(t, m, i, j);
-            const double v = abs2(S[(r + i) * N + r + j]);
-            if (v > best) {
-                best = v;
+            const zc z = S[(r + i) * N + r + j];
+            const unsigned long long kx = (unsigned long long)__double_as_longlong(z.x) & 0x7fffffffffffffffull;
+            const unsigned long long ky = (unsigned long long)__double_as_longlong(z.y) & 0x7fffffffffffffffull;
+            const unsigned long long key = kx > ky ? kx : ky;
+            if (key > best || bidx == 0x7fffffff) {
+                best = key;
                 bidx = t;
             }
         }
-        block_argmax(best, bidx, red);
-        if (bidx == 0x7fffffff) {  // only non-finite entries left: no pivot exists
+        block_argmax_u64(best, bidx, red);
+        if (bidx == 0x7fffffff) {  // no candidate: cannot happen for T >= 1
             underflow = 2;
             return mk(0.0, 0.0);
         }
@@ -211,6 +216,11 @@ __device__ zc pfaffian_upper(zc *S, int N, zc *vec, double *red, int &underflow)
         if (i1 != r) exch_upper(S, N, r, r, i1);
         if (i2 != c) exch_upper(S, N, r, c, i2);
         const zc ss = S[r * N + c];
+        if (!zfinite(ss)) {
+            underflow = 2;
+            __syncthreads();
+            return mk(0.0, 0.0);
+        }
         if (!(abs2(ss) > 1.0e-26)) {
             underflow = 1;
             __syncthreads();
@@ -426,13 +436,14 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                 const zc en = expi(phn);
                 // ---- S = Cscale [[D X D, -I], [I, -Z0]] (upper triangle)
                 const double cs = p.cscale;
+                const zc dpp = cs * (ep * ep), dpn = cs * (ep * en), dnn = cs * (en * en);
                 for (int t = threadIdx.x; t < N * (N - 1) / 2; t += blockDim.x) {
                     int i, j;
                     tri_index(t, N, i, j);
                     zc v;
                     if (j < n) {
-                        const zc dd = ((i < h) ? ep : en) * ((j < h) ? ep : en);
-                        v = cs * (X[i * n + j] * dd);
+                        const zc dd = (j < h) ? dpp : ((i < h) ? dpn : dnn);
+                        v = X[i * n + j] * dd;
                     } else if (i < n) {
                         v = mk((j - n == i) ? -cs : 0.0, 0.0);
                     } else {
@@ -467,6 +478,16 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     S[t] = (q == 2) ? -(zconj(di) * s) : di * s;
                 }
                 __syncthreads();
+                // antisymmetrised pairing tensors in the free quarter of S:
+                // K01_ij (i < j) at Kc[i n + j], K10_ij at Kc[j n + i]
+                zc *Kc = S + 3 * nn;
+                for (int t = threadIdx.x; t < n * (n - 1) / 2; t += blockDim.x) {
+                    int i, j;
+                    tri_index(t, n, i, j);
+                    Kc[i * n + j] = k01[i * n + j] - k01[j * n + i];
+                    Kc[j * n + i] = k10[i * n + j] - k10[j * n + i];
+                }
+                __syncthreads();
                 // ---- observables (18 complex partial sums)
                 double part[kNPart];
 #pragma unroll
@@ -477,6 +498,19 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     else { part[2] += d.x; part[3] += d.y; }
                     part[8] = fma(p.obs.jj1[a], d.x, part[8]);
                     part[9] = fma(p.obs.jj1[a], d.y, part[9]);
+                    const double jpa = p.obs.jp[a], jma = p.obs.jm[a], mza = p.obs.mz[a];
+                    if (jpa != 0.0) {
+                        const zc r = rho[(a + 1) * n + a];
+                        part[10] = fma(jpa, r.x, part[10]);
+                        part[11] = fma(jpa, r.y, part[11]);
+                    }
+                    if (jma != 0.0) {
+                        const zc r = rho[(a - 1) * n + a];
+                        part[12] = fma(jma, r.x, part[12]);
+                        part[13] = fma(jma, r.y, part[13]);
+                    }
+                    part[14] = fma(mza, d.x, part[14]);
+                    part[15] = fma(mza, d.y, part[15]);
                 }
                 for (int e = threadIdx.x; e < p.obs.n_t1b; e += blockDim.x) {
                     const zc r = rho[p.obs.t1b_idx[e]];
@@ -494,15 +528,11 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                         const double v = p.rec_v[e];
                         zc t = rho[k * n + i] * rho[l * n + j];
                         t = zfms(rho[l * n + i], rho[k * n + j], t);
-                        const zc K01ij = k01[i * n + j] - k01[j * n + i];
-                        const zc K10kl = k10[k * n + l] - k10[l * n + k];
-                        zc u = K01ij * K10kl;
+                        zc u = Kc[i * n + j] * Kc[l * n + k];
                         if (i + j != k + l) {
                             t = zfma(rho[i * n + k], rho[j * n + l], t);
                             t = zfms(rho[j * n + k], rho[i * n + l], t);
-                            const zc K01kl = k01[k * n + l] - k01[l * n + k];
-                            const zc K10ij = k10[i * n + j] - k10[j * n + i];
-                            u = zfma(K01kl, K10ij, u);
+                            u = zfma(Kc[k * n + l], Kc[j * n + i], u);
                         }
                         t = rfma(0.25, u, t);
                         e2 = rfma(v, t, e2);
@@ -510,35 +540,22 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     part[6] += e2.x;
                     part[7] += e2.y;
                 }
-                // <J^2> (ZJ2_0, PNAMP_ME2B.f90:45-147): sum_axes Tr(J^2 rho) [above,
-                // via j(j+1)] + Tr(J rho)^2 - Tr(J rho J rho) + Tr(J k10 J^T k01^T)
-                for (int ax = 0; ax < 3; ++ax) {
-                    const int *jrc = p.obs.jr_col + ax * 2 * n;
-                    const zc *jrv = p.obs.jr_val + ax * 2 * n;
-                    const int *jcr = p.obs.jc_row + ax * 2 * n;
-                    const zc *jcv = p.obs.jc_val + ax * 2 * n;
-                    zc tr2 = mk(0, 0), rest = mk(0, 0);
+                {   // <J^2> (ZJ2_0, PNAMP_ME2B.f90:45-147) summed over x, y, z with
+                    // Jx, Jy = (J+ +- J-)/(2, 2i):  sum_a j(j+1) rho_aa [above]
+                    // + Tr(J+ rho) Tr(J- rho) + Tr(Jz rho)^2 - Tr(J+ rho J- rho) - Tr(Jz rho Jz rho)
+                    // + [Tr(J+ k10 J+ k01^T) + Tr(J- k10 J- k01^T)]/2 + Tr(Jz k10 Jz k01^T)
+                    zc rest = mk(0, 0);
                     for (int t = threadIdx.x; t < nn; t += blockDim.x) {
                         const int a = t / n, c = t % n;
-                        zc mac = mk(0, 0), mca = mk(0, 0), jk = mk(0, 0), kj = mk(0, 0);
-#pragma unroll
-                        for (int q = 0; q < 2; ++q) {
-                            const int b1 = jrc[2 * a + q];
-                            if (b1 >= 0) {
-                                mac = zfma(jrv[2 * a + q], rho[b1 * n + c], mac);
-                                jk = zfma(jrv[2 * a + q], k10[b1 * n + c], jk);
-                            }
-                            const int b2 = jrc[2 * c + q];
-                            if (b2 >= 0) mca = zfma(jrv[2 * c + q], rho[b2 * n + a], mca);
-                            const int b3 = jcr[2 * c + q];
-                            if (b3 >= 0) kj = zfma(k01[a * n + b3], jcv[2 * c + q], kj);
-                        }
-                        rest = zfms(mac, mca, rest);
-                        rest = zfma(jk, kj, rest);
-                        if (c == a) tr2 = tr2 + mac;
+                        const double jpa = p.obs.jp[a], jma = p.obs.jm[a], jpc = p.obs.jp[c], jmc = p.obs.jm[c];
+                        const double mzz = p.obs.mz[a] * p.obs.mz[c];
+                        zc q = mzz * (k10[t] * k01[t]);
+                        q = zfms(mzz * rho[t], rho[c * n + a], q);
+                        if (jpa != 0.0 && jmc != 0.0) q = zfms((jpa * jmc) * rho[(a + 1) * n + c], rho[(c - 1) * n + a], q);
+                        if (jpa != 0.0 && jpc != 0.0) q = zfma((0.5 * jpa * jpc) * k10[(a + 1) * n + c], k01[a * n + c + 1], q);
+                        if (jma != 0.0 && jmc != 0.0) q = zfma((0.5 * jma * jmc) * k10[(a - 1) * n + c], k01[a * n + c - 1], q);
+                        rest = rest + q;
                     }
-                    part[10 + 2 * ax] += tr2.x;
-                    part[11 + 2 * ax] += tr2.y;
                     part[8] += rest.x;
                     part[9] += rest.y;
                 }
@@ -561,9 +578,9 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     const zc norm = (p.vacfac * det0 * det1) * (pf * zph);
                     const zc zp = mk(part[0], part[1]), zn = mk(part[2], part[3]);
                     const zc ekin = mk(part[4], part[5]), e2 = mk(part[6], part[7]);
-                    const zc t2x = mk(part[10], part[11]), t2y = mk(part[12], part[13]),
-                             t2z = mk(part[14], part[15]);
-                    const zc j2 = mk(part[8], part[9]) + t2x * t2x + t2y * t2y + t2z * t2z;
+                    const zc trp = mk(part[10], part[11]), trm = mk(part[12], part[13]),
+                             trz = mk(part[14], part[15]);
+                    const zc j2 = mk(part[8], part[9]) + trp * trm + trz * trz;
                     acc[0] = acc[0] + norm;
                     int f = (under == 1) ? 1 : (under == 2 ? 4 : 0);
                     if (sing) {
