@@ -153,6 +153,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--form", default="fp64", choices=["fp64", "df64"],
+                    help="arithmetic of the per-point algebra: plain FP64 or double-float")
     ap.add_argument("--mesh", default=None,
                     help="override the mesh as NALP,NBET,NGAM,NFOM (small cases for profiling captures)")
     args = ap.parse_args()
@@ -211,7 +213,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    ctx = PnampContext(wl.sp, wl.e0, wl.t1b, wl.recs, wl.vbar, wl.mesh, q2=wl.q2)
+    ctx = PnampContext(wl.sp, wl.e0, wl.t1b, wl.recs, wl.vbar, wl.mesh, q2=wl.q2, form=args.form)
     P = ctx.n_euler
     G = wl.mesh.n_gauge
     pts_per_pair = P * G

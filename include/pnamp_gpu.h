@@ -49,6 +49,12 @@ extern "C" {
 /* Size of the fixed device scratch array used by pnamp_batch_device_noalloc. */
 #define PNAMP_NOALLOC_SCRATCH_BYTES (32u << 20)
 
+/* arithmetic forms of the per-point algebra (pnamp_set_form) */
+#define PNAMP_FORM_FP64 0   /* FP64 throughout: the reference's arithmetic (default) */
+#define PNAMP_FORM_DF64 1   /* Pfaffian, LU, solves, densities and contractions in double-float
+                               (pairs of FP32, ~48-bit significand) on the FP32 pipes; per-Euler
+                               preparation, the Pfaffian product and all reductions stay FP64 */
+
 /* per-Euler-point status bits (OR over the gauge points of that Euler point) */
 #define PNAMP_ST_PIVOT_UNDERFLOW 1  /* Pfaffian pivot |ss| <= 1e-13: norm set to 0 (PNAMP_Proj.f90:290,333) */
 #define PNAMP_ST_SINGULAR_T22 2     /* exact zero pivot in the LU of T22 */
@@ -102,6 +108,10 @@ typedef struct pnamp_ctx pnamp_ctx;
  * projection weights. Replaces the one-off part of PNAMP_Main.f90:27-50. */
 int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h,
                const pnamp_mesh *m, pnamp_ctx **out);
+
+/* Select the arithmetic form of later pnamp_pair/batch calls (PNAMP_FORM_*).
+ * No counterpart in the reference, which computes in FP64 only. */
+int pnamp_set_form(pnamp_ctx *ctx, int form);
 
 /* Number of Euler points P_E of the context's mesh (rows of ZRES). */
 int pnamp_n_euler(const pnamp_ctx *ctx);

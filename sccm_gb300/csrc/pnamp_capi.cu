@@ -27,6 +27,7 @@ struct pnamp_ctx {
     int core_prot, core_neut;
     int axial;
     int grid;
+    int grid_form[2];
     std::vector<void *> allocs;
     double *d_pairbuf = nullptr;
     long long pair_cap = 0;
@@ -61,6 +62,19 @@ int dev_upload(pnamp_ctx *c, const std::vector<T> &h, const T **out) {
     if (!h.empty()) CK(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
     *out = d;
     return PNAMP_OK;
+}
+
+dd host_dd(double x) {
+    dd r;
+    r.hi = (float)x;
+    r.lo = (float)(x - (double)r.hi);
+    return r;
+}
+
+std::vector<dd> to_dd(const std::vector<double> &v) {
+    std::vector<dd> out(v.size());
+    for (size_t i = 0; i < v.size(); ++i) out[i] = host_dd(v[i]);
+    return out;
 }
 
 int plan_placement(Params &p, int smem_max) {
@@ -151,6 +165,12 @@ const char *pnamp_strerror(int code) {
 const char *pnamp_version(void) { return "sccm_gb300 pnamp 0.1 (sm_103a, fp64)"; }
 
 int pnamp_n_euler(const pnamp_ctx *ctx) { return ctx ? ctx->p.n_euler : -1; }
+
+int pnamp_set_form(pnamp_ctx *ctx, int form) {
+    if (!ctx || (form != PNAMP_FORM_FP64 && form != PNAMP_FORM_DF64)) return PNAMP_ERR_ARG;
+    ctx->p.form = form;
+    return PNAMP_OK;
+}
 
 void pnamp_free(pnamp_ctx *ctx) {
     if (!ctx) return;
@@ -310,6 +330,8 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
     UP(fact, p.fact);
     UP(rec_idx, p.rec_idx);
     UP(rec_v, p.rec_v);
+    const std::vector<dd> rec_vd = to_dd(rec_v), jp_d = to_dd(jpv), jm_d = to_dd(jmv), mz_d = to_dd(mzv);
+    UP(rec_vd, p.rec_vd);
     ot.n_t1b = (int)t1b_idx.size();
     UP(t1b_idx, ot.t1b_idx);
     UP(t1b_val, ot.t1b_val);
@@ -319,6 +341,9 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
     UP(jmv, ot.jm);
     UP(mzv, ot.mz);
     UP(jj1, ot.jj1);
+    UP(jp_d, ot.jp_d);
+    UP(jm_d, ot.jm_d);
+    UP(mz_d, ot.mz_d);
 #undef UP
     p.obs = ot;
     int smem_optin = 0, nsm = 0;
@@ -331,16 +356,17 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
         pnamp_free(c);
         return rc;
     }
-    if (set_point_smem(p.place.smem_bytes) != cudaSuccess) {
-        pnamp_free(c);
-        return PNAMP_ERR_CUDA;
+    for (int form = 0; form < 2; ++form) {
+        int per_sm = 0;
+        if (set_point_smem(form, p.place.smem_bytes) != cudaSuccess ||
+            point_blocks_per_sm(form, p.place.smem_bytes, &per_sm) != cudaSuccess || per_sm < 1) {
+            pnamp_free(c);
+            return PNAMP_ERR_CUDA;
+        }
+        c->grid_form[form] = nsm * per_sm;
     }
-    int per_sm = 0;
-    if (point_blocks_per_sm(p.place.smem_bytes, &per_sm) != cudaSuccess || per_sm < 1) {
-        pnamp_free(c);
-        return PNAMP_ERR_CUDA;
-    }
-    c->grid = nsm * per_sm;
+    p.form = 0;
+    c->grid = std::max(c->grid_form[0], c->grid_form[1]);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         pnamp_free(c);
         return PNAMP_ERR_CUDA;
@@ -369,7 +395,7 @@ int pnamp_batch_device(pnamp_ctx *c, int npairs, const double *d_uv, double *d_z
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
     CK(launch_setup(c->p, npairs, d_uv, c->d_pairbuf, st));
-    CK(launch_points(c->p, npairs, c->d_pairbuf, c->d_scratch, c->grid, d_zres, d_status, st));
+    CK(launch_points(c->p, npairs, c->d_pairbuf, c->d_scratch, c->grid_form[c->p.form], d_zres, d_status, st));
     return PNAMP_OK;
 }
 
@@ -483,7 +509,7 @@ extern "C" int pnamp_batch_device_noalloc(pnamp_ctx *c, int npairs, const double
     const unsigned long long slot_bytes = (unsigned long long)c->p.place.slot_elems * sizeof(zc);
     if (pair_bytes + slot_bytes > cap) return PNAMP_ERR_SCRATCH_LIMIT;
     const unsigned long long fit = (cap - pair_bytes) / slot_bytes;
-    const int grid = (int)std::min<unsigned long long>((unsigned long long)c->grid, fit);
+    const int grid = (int)std::min<unsigned long long>((unsigned long long)c->grid_form[c->p.form], fit);
     void *base = nullptr;
     const int rc = noalloc_scratch(&base);
     if (rc) return rc;

@@ -4,7 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "pnamp_device.cuh"
+#include "pnamp_df64.cuh"
 
 namespace pnamp {
 
@@ -53,6 +53,7 @@ struct ObsTables {
     const double *jm;          // [n] J-_{a,a-1} (0 at the first state of a block)
     const double *mz;          // [n] m_a
     const double *jj1;         // [n] j(j+1)
+    const dd *jp_d, *jm_d, *mz_d;   // the same coefficients as double-float
 };
 
 struct Params {
@@ -63,6 +64,7 @@ struct Params {
     double e0;                 // H%E0, added to every energy (Kernel3D.f90:324)
     double vacfac;             // (-1)^{n(n+1)/2} * 10^(-2*(n*iscale/2))
     int iE2;
+    int form;                  // 0: FP64 (plain), 1: double-float per-point algebra
     // rotation blocks
     int nblk, rot_elems;
     const int *blk_start, *blk_size, *blk_tj, *blk_roff, *row_blk, *twom;
@@ -72,6 +74,7 @@ struct Params {
     int nrec;
     const uint32_t *rec_idx;   // packed 8-bit a,b,c,d (0-based)
     const double *rec_v;
+    const dd *rec_vd;          // rec_v as double-float (df64 form)
     ObsTables obs;
     PairLayout pl;
     Placement place;
@@ -85,8 +88,8 @@ cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc
 cudaError_t launch_proj_weights(const Params &p, int axial, zc *w, cudaStream_t st);
 cudaError_t launch_project(const Params &p, int npairs, const zc *w, const double *zres,
                            int core_prot, int core_neut, int chop, double *out, cudaStream_t st);
-cudaError_t set_point_smem(int bytes);
-cudaError_t point_blocks_per_sm(int smem_bytes, int *per_sm);
+cudaError_t set_point_smem(int form, int bytes);
+cudaError_t point_blocks_per_sm(int form, int smem_bytes, int *per_sm);
 int setup_smem_bytes(int n);
 
 }  // namespace pnamp

@@ -25,6 +25,7 @@
 //   T22 = V0^T A V1 + U0^T A* U1 = sum_s e^{+-i phi_s} (species partials),
 //   rho = D (R V1 T22^-1) V0^T, kappa10 = D (R V1 T22^-1) U0^T,
 //   kappa01 = -D* (R* U1 T22^-1) V0^T.
+#include "pnamp_df64.cuh"
 #include "pnamp_internal.h"
 
 namespace pnamp {
@@ -41,6 +42,45 @@ __device__ __forceinline__ zc sfms(zc a, zc b, zc c) { return zfms(a, b, c); }
 template <typename T> __device__ __forceinline__ T szero();
 template <> __device__ __forceinline__ double szero<double>() { return 0.0; }
 template <> __device__ __forceinline__ zc szero<zc>() { return mk(0.0, 0.0); }
+__device__ __forceinline__ double sabs1(zd a) { return (double)(fabsf(a.x.hi) + fabsf(a.y.hi)); }
+__device__ __forceinline__ zd srecip(zd a) { return zrecip(a); }
+__device__ __forceinline__ zd smul(zd a, zd b) { return a * b; }
+__device__ __forceinline__ zd sfms(zd a, zd b, zd c) { return zfms(a, b, c); }
+template <> __device__ __forceinline__ zd szero<zd>() { return mkd(dd_make(0.0f, 0.0f), dd_make(0.0f, 0.0f)); }
+
+// Arithmetic traits of the per-point algebra: zc = FP64 complex (plain form),
+// zd = double-float complex (df64 form). R is the matching real type.
+template <class Z> struct Ar;
+template <> struct Ar<zc> {
+    using R = double;
+    static __device__ __forceinline__ zc from(zc a) { return a; }
+    static __device__ __forceinline__ zc to(zc a) { return a; }
+    static __device__ __forceinline__ R real(double v) { return v; }
+    static __device__ __forceinline__ R rmul(R a, R b) { return a * b; }
+    static __device__ __forceinline__ bool nz(R a) { return a != 0.0; }
+    static __device__ __forceinline__ R pick(const double *d, const dd *, long long i) { return d[i]; }
+    // pivot key: max(|re|, |im|) as the bit pattern of a non-negative double
+    static __device__ __forceinline__ unsigned long long key(zc z) {
+        const unsigned long long kx = (unsigned long long)__double_as_longlong(z.x) & 0x7fffffffffffffffull;
+        const unsigned long long ky = (unsigned long long)__double_as_longlong(z.y) & 0x7fffffffffffffffull;
+        return kx > ky ? kx : ky;
+    }
+};
+template <> struct Ar<zd> {
+    using R = dd;
+    static __device__ __forceinline__ zd from(zc a) { return zd_from(a); }
+    static __device__ __forceinline__ zc to(zd a) { return zd_to(a); }
+    static __device__ __forceinline__ R real(double v) { return dd_from(v); }
+    static __device__ __forceinline__ R rmul(R a, R b) { return dd_mul(a, b); }
+    static __device__ __forceinline__ bool nz(R a) { return a.hi != 0.0f; }
+    static __device__ __forceinline__ R pick(const double *, const dd *f, long long i) { return f[i]; }
+    static __device__ __forceinline__ unsigned long long key(zd z) {
+        const unsigned int kx = __float_as_uint(z.x.hi) & 0x7fffffffu;
+        const unsigned int ky = __float_as_uint(z.y.hi) & 0x7fffffffu;
+        return kx > ky ? kx : ky;
+    }
+};
+
 
 // Pivot row for column k (largest |re|+|im|, first on ties, as IZAMAX): warp 0
 // searches, the result is broadcast through sh[0] (row) and sh[1] (zero column).
@@ -152,18 +192,19 @@ __device__ void row_solve(T *Y, int nr, int ldy, const T *A, int n, int lda, con
 // ------------------------------------------------------------------ Pfaffian
 // Exchange of indices p < q of a skew matrix held in its upper triangle, rows
 // >= r only (ZExch, PNAMP_Proj.f90:356-392). Every thread touches distinct entries.
-__device__ __forceinline__ void exch_upper(zc *S, int N, int r, int p, int q) {
+template <class Z>
+__device__ __forceinline__ void exch_upper(Z *S, int N, int r, int p, int q) {
     for (int i = r + threadIdx.x; i < N; i += blockDim.x) {
         if (i < p) {
-            const zc t = S[i * N + p];
+            const Z t = S[i * N + p];
             S[i * N + p] = S[i * N + q];
             S[i * N + q] = t;
         } else if (i > q) {
-            const zc t = S[p * N + i];
+            const Z t = S[p * N + i];
             S[p * N + i] = S[q * N + i];
             S[q * N + i] = t;
         } else if (i > p && i < q) {
-            const zc t = S[p * N + i];
+            const Z t = S[p * N + i];
             S[p * N + i] = -S[i * N + q];
             S[i * N + q] = -t;
         } else if (i == p) {
@@ -174,28 +215,26 @@ __device__ __forceinline__ void exch_upper(zc *S, int N, int r, int p, int q) {
 }
 
 // Pfaffian of the N x N skew matrix in the upper triangle of S (row-major),
-// ZPfaffianF (PNAMP_Proj.f90:218-350): at each 2x2 step the largest |S_ij| of
-// the remaining upper triangle (row-major scan, first maximum) is moved to
-// (r, r+1), the sign flips once per exchange, Pf = 0 when |pivot| <= 1e-13,
-// and the Schur complement is updated in place. `vec` holds N scratch values.
-__device__ zc pfaffian_upper(zc *S, int N, zc *vec, double *red, int &underflow) {
+// ZPfaffianF (PNAMP_Proj.f90:218-350): at each 2x2 step the largest entry of the
+// remaining upper triangle (row-major scan, first maximum; magnitude max(|re|,|im|))
+// is moved to (r, r+1), the sign flips once per exchange, Pf = 0 when
+// |pivot| <= 1e-13, and the Schur complement is updated in place. The running
+// product is kept in FP64. `vec` holds N scratch values.
+template <class Z>
+__device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int &underflow) {
+    using A = Ar<Z>;
     zc pf = mk(1.0, 0.0);
     underflow = 0;
     const int NB = N / 2;
     for (int k = 0; k < NB - 1; ++k) {
         const int r = 2 * k, c = r + 1, m = N - r;
         const int T = m * (m - 1) / 2;
-        // pivot key: max(|re|, |im|) compared as the integer bit patterns of
-        // non-negative doubles (exact order, no FP64 instructions)
         unsigned long long best = 0ull;
         int bidx = 0x7fffffff;
         for (int t = threadIdx.x; t < T; t += blockDim.x) {
             int i, j;
             tri_index(t, m, i, j);
-            const zc z = S[(r + i) * N + r + j];
-            const unsigned long long kx = (unsigned long long)__double_as_longlong(z.x) & 0x7fffffffffffffffull;
-            const unsigned long long ky = (unsigned long long)__double_as_longlong(z.y) & 0x7fffffffffffffffull;
-            const unsigned long long key = kx > ky ? kx : ky;
+            const unsigned long long key = A::key(S[(r + i) * N + r + j]);
             if (key > best || bidx == 0x7fffffff) {
                 best = key;
                 bidx = t;
@@ -215,7 +254,8 @@ __device__ zc pfaffian_upper(zc *S, int N, zc *vec, double *red, int &underflow)
         if (i2 == c) phas = -phas;
         if (i1 != r) exch_upper(S, N, r, r, i1);
         if (i2 != c) exch_upper(S, N, r, c, i2);
-        const zc ss = S[r * N + c];
+        const Z ssz = S[r * N + c];
+        const zc ss = A::to(ssz);
         if (!zfinite(ss)) {
             underflow = 2;
             __syncthreads();
@@ -226,7 +266,7 @@ __device__ zc pfaffian_upper(zc *S, int N, zc *vec, double *red, int &underflow)
             __syncthreads();
             return mk(0.0, 0.0);
         }
-        const zc inv = zrecip(ss);
+        const Z inv = zrecip(ssz);
         for (int i = c + 1 + threadIdx.x; i < N; i += blockDim.x) vec[i] = S[c * N + i] * inv;
         __syncthreads();
         const int mm = N - c - 1, TT = mm * (mm - 1) / 2;
@@ -235,7 +275,7 @@ __device__ zc pfaffian_upper(zc *S, int N, zc *vec, double *red, int &underflow)
             tri_index(t, mm, i, j);
             i += c + 1;
             j += c + 1;
-            zc s = S[i * N + j];
+            Z s = S[i * N + j];
             s = zfma(vec[i], S[r * N + j], s);
             s = zfms(S[r * N + i], vec[j], s);
             S[i * N + j] = s;
@@ -243,7 +283,7 @@ __device__ zc pfaffian_upper(zc *S, int N, zc *vec, double *red, int &underflow)
         pf = phas * (pf * ss);
         __syncthreads();
     }
-    pf = pf * S[(N - 2) * N + N - 1];
+    pf = pf * A::to(S[(N - 2) * N + N - 1]);
     __syncthreads();
     return pf;
 }
@@ -319,32 +359,36 @@ cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *
 // ------------------------------------------------------------------ points
 constexpr int kNPart = 36;  // 18 complex partial sums per gauge point
 
+template <class Z>
 __global__ void __launch_bounds__(kThreads, 1)
 point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scratch,
              double *__restrict__ zres, int *__restrict__ status) {
+    using A = Ar<Z>;
+    using R = typename A::R;
     extern __shared__ __align__(16) unsigned char smem[];
     const int n = p.n, h = p.h, N = p.N2;
     const int nn = n * n;
     const Placement &pl = p.place;
     zc *slot = scratch + (long long)blockIdx.x * pl.slot_elems;
-    zc *X = slot + pl.g_x;    // R W R^T
-    zc *B = slot + pl.g_b;    // rows 0..n-1: R V1, rows n..2n-1: conj(R) U1
-    zc *P = slot + pl.g_p;    // T22 partials: V0p, V0n, U0p, U0n
-    zc *RW = slot + pl.g_rw;  // R W
-    zc *S = pl.s_smem ? reinterpret_cast<zc *>(smem + pl.off_s) : slot + pl.g_s;
-    zc *T = pl.t_smem ? reinterpret_cast<zc *>(smem + pl.off_t) : slot + pl.g_t;
-    zc *Y = pl.y_smem ? reinterpret_cast<zc *>(smem + pl.off_y) : slot + pl.g_y;
-    double *V0s = pl.uv_smem ? reinterpret_cast<double *>(smem + pl.off_uv)
-                             : reinterpret_cast<double *>(slot + pl.g_uv);
-    double *U0s = V0s + nn;
+    Z *X = reinterpret_cast<Z *>(slot + pl.g_x);    // R W R^T
+    Z *B = reinterpret_cast<Z *>(slot + pl.g_b);    // rows 0..n-1: R V1, rows n..2n-1: conj(R) U1
+    zc *Bz = slot + pl.g_b;                         // the same storage while it holds FP64 values
+    Z *P = reinterpret_cast<Z *>(slot + pl.g_p);    // T22 partials: V0p, V0n, U0p, U0n
+    zc *RW = slot + pl.g_rw;                        // R W
+    Z *S = reinterpret_cast<Z *>(pl.s_smem ? (void *)(smem + pl.off_s) : (void *)(slot + pl.g_s));
+    Z *T = reinterpret_cast<Z *>(pl.t_smem ? (void *)(smem + pl.off_t) : (void *)(slot + pl.g_t));
+    Z *Y = reinterpret_cast<Z *>(pl.y_smem ? (void *)(smem + pl.off_y) : (void *)(slot + pl.g_y));
+    R *V0s = reinterpret_cast<R *>(pl.uv_smem ? (void *)(smem + pl.off_uv) : (void *)(slot + pl.g_uv));
+    R *U0s = V0s + nn;
     int *perm = reinterpret_cast<int *>(smem + pl.off_piv);
     int *sh = perm + n;
-    zc *invd = reinterpret_cast<zc *>(smem + pl.off_inv);
+    Z *invd = reinterpret_cast<Z *>(smem + pl.off_inv);
     double *red = reinterpret_cast<double *>(smem + pl.off_red);
     zc *rot = reinterpret_cast<zc *>(smem + pl.off_rot);
-    zc *vec = reinterpret_cast<zc *>(smem + pl.off_vec);
-    zc *acc = vec + N;  // kNobs accumulators
-    zc *rho = S, *k10 = S + nn, *k01 = S + 2 * nn;
+    Z *vec = reinterpret_cast<Z *>(smem + pl.off_vec);
+    zc *acc = reinterpret_cast<zc *>(vec + N);  // kNobs accumulators
+    Z *rho = S, *k10 = S + nn, *k01 = S + 2 * nn;
+    Z *Kc = S + 3 * nn;  // antisymmetrised pairing tensors
 
     const long long total = (long long)npairs * p.n_euler;
     const double twopi = 6.283185307179586476925287;
@@ -352,7 +396,7 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
     for (long long item = blockIdx.x; item < total; item += gridDim.x) {
         const int pair = (int)(item / p.n_euler), ie = (int)(item % p.n_euler);
         const double *pr = pairbuf + (long long)pair * p.pl.stride;
-        const double *gU1 = pr + p.pl.u1, *gV1 = pr + p.pl.v1;
+        const double *gU1 = pr + p.pl.u1, *gV1 = pr + p.pl.v1, *gU0 = pr + p.pl.u0, *gV0 = pr + p.pl.v0;
         const double *gW = pr + p.pl.w, *gZ0 = pr + p.pl.z0;
         const double det0 = pr[p.pl.dets], det1 = pr[p.pl.dets + 1];
         const int pst = (int)pr[p.pl.dets + 2];
@@ -368,12 +412,12 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
         if (pair != cur_pair) {
             __syncthreads();
             for (int t = threadIdx.x; t < nn; t += blockDim.x) {
-                V0s[t] = pr[p.pl.v0 + t];
-                U0s[t] = pr[p.pl.u0 + t];
+                V0s[t] = A::real(gV0[t]);
+                U0s[t] = A::real(gU0[t]);
             }
             cur_pair = pair;
         }
-        // ---- rotation blocks R_b(i,k) = e^{-i alp m_i} d^j_{m_i m_k}(bet) e^{-i gam m_k}
+        // ---- rotation blocks R_b(i,k) = e^{-i alp m_i} d^j_{m_i m_k}(bet) e^{-i gam m_k}  (FP64)
         const double alp = p.euler[4 * ie], bet = p.euler[4 * ie + 1], gam = p.euler[4 * ie + 2];
         double cb, sb;
         sincos(0.5 * bet, &sb, &cb);
@@ -390,7 +434,7 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
             for (int io = 0; io < kNobs; ++io) acc[io] = mk(0.0, 0.0);
         }
         __syncthreads();
-        // ---- R W, R V1, conj(R) U1
+        // ---- R W, R V1, conj(R) U1 (FP64)
         for (int t = threadIdx.x; t < nn; t += blockDim.x) {
             const int a = t / n, j = t % n;
             const int b = p.row_blk[a], s0 = p.blk_start[b], d = p.blk_size[b];
@@ -403,27 +447,32 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                 b2 = rfma(gU1[(s0 + k) * n + j], zconj(r), b2);
             }
             RW[t] = rw;
-            B[t] = b1;
-            B[nn + t] = b2;
+            Bz[t] = b1;
+            Bz[nn + t] = b2;
         }
         __syncthreads();
-        // ---- X = (R W) R^T and the T22 partials
+        // ---- X = (R W) R^T and the T22 partials (FP64), stored in the point arithmetic
         for (int t = threadIdx.x; t < nn; t += blockDim.x) {
             const int a = t / n, c = t % n;
             const int b = p.row_blk[c], s0 = p.blk_start[b], d = p.blk_size[b];
             const zc *Rr = rot + p.blk_roff[b] + (c - s0) * d;
             zc x = mk(0, 0);
             for (int k = 0; k < d; ++k) x = zfma(RW[a * n + s0 + k], Rr[k], x);
-            X[t] = x;
+            X[t] = A::from(x);
         }
         for (int t = threadIdx.x; t < 4 * nn; t += blockDim.x) {
             const int q = t / nn, e = t % nn, i = e / n, j = e % n;
-            const double *M = (q < 2) ? V0s : U0s;
-            const zc *Bq = (q < 2) ? B : B + nn;
+            const double *M = (q < 2) ? gV0 : gU0;
+            const zc *Bq = (q < 2) ? Bz : Bz + nn;
             const int k0 = (q & 1) ? h : 0;
             zc s = mk(0, 0);
             for (int k = k0; k < k0 + h; ++k) s = rfma(M[k * n + i], Bq[k * n + j], s);
-            P[t] = s;
+            P[t] = A::from(s);
+        }
+        __syncthreads();
+        for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) {  // in place, element by element
+            const zc v = Bz[t];
+            B[t] = A::from(v);
         }
         __syncthreads();
 
@@ -436,51 +485,50 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                 const zc en = expi(phn);
                 // ---- S = Cscale [[D X D, -I], [I, -Z0]] (upper triangle)
                 const double cs = p.cscale;
-                const zc dpp = cs * (ep * ep), dpn = cs * (ep * en), dnn = cs * (en * en);
+                const Z dpp = A::from(cs * (ep * ep)), dpn = A::from(cs * (ep * en)), dnn = A::from(cs * (en * en));
+                const Z mcs = A::from(mk(-cs, 0.0)), zero = A::from(mk(0.0, 0.0));
                 for (int t = threadIdx.x; t < N * (N - 1) / 2; t += blockDim.x) {
                     int i, j;
                     tri_index(t, N, i, j);
-                    zc v;
+                    Z v;
                     if (j < n) {
-                        const zc dd = (j < h) ? dpp : ((i < h) ? dpn : dnn);
-                        v = X[i * n + j] * dd;
+                        const Z dd_ = (j < h) ? dpp : ((i < h) ? dpn : dnn);
+                        v = X[i * n + j] * dd_;
                     } else if (i < n) {
-                        v = mk((j - n == i) ? -cs : 0.0, 0.0);
+                        v = (j - n == i) ? mcs : zero;
                     } else {
-                        v = mk(-cs * gZ0[(i - n) * n + (j - n)], 0.0);
+                        v = A::from(mk(-cs * gZ0[(i - n) * n + (j - n)], 0.0));
                     }
                     S[i * N + j] = v;
                 }
                 __syncthreads();
                 int under;
-                const zc pf = pfaffian_upper(S, N, vec, red, under);
+                const zc pf = pfaffian_upper<Z>(S, N, vec, red, under);
                 // ---- T22(phi) and right-hand sides
-                const zc epc = zconj(ep), enc = zconj(en);
+                const Z zep = A::from(ep), zen = A::from(en), zepc = A::from(zconj(ep)), zenc = A::from(zconj(en));
                 for (int t = threadIdx.x; t < nn; t += blockDim.x) {
-                    zc s = ep * P[t];
-                    s = zfma(en, P[nn + t], s);
-                    s = zfma(epc, P[2 * nn + t], s);
-                    s = zfma(enc, P[3 * nn + t], s);
+                    Z s = zep * P[t];
+                    s = zfma(zen, P[nn + t], s);
+                    s = zfma(zepc, P[2 * nn + t], s);
+                    s = zfma(zenc, P[3 * nn + t], s);
                     T[t] = s;
                 }
                 for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) Y[t] = B[t];
                 __syncthreads();
-                const bool sing = lu_factor<zc>(T, n, n, perm, invd, sh);
-                row_solve<zc>(Y, 2 * n, n, T, n, n, perm, invd);
+                const bool sing = lu_factor<Z>(T, n, n, perm, invd, sh);
+                row_solve<Z>(Y, 2 * n, n, T, n, n, perm, invd);
                 // ---- densities into the Pfaffian's storage
                 for (int t = threadIdx.x; t < 3 * nn; t += blockDim.x) {
                     const int q = t / nn, e = t % nn, i = e / n, j = e % n;
-                    const zc *Yr = (q == 2) ? Y + (n + i) * n : Y + i * n;
-                    const double *M = (q == 1) ? U0s + j * n : V0s + j * n;
-                    zc s = mk(0, 0);
+                    const Z *Yr = (q == 2) ? Y + (n + i) * n : Y + i * n;
+                    const R *M = (q == 1) ? U0s + j * n : V0s + j * n;
+                    Z s = zero;
                     for (int k = 0; k < n; ++k) s = rfma(M[k], Yr[k], s);
-                    const zc di = (i < h) ? ep : en;
+                    const Z di = (i < h) ? zep : zen;
                     S[t] = (q == 2) ? -(zconj(di) * s) : di * s;
                 }
                 __syncthreads();
-                // antisymmetrised pairing tensors in the free quarter of S:
                 // K01_ij (i < j) at Kc[i n + j], K10_ij at Kc[j n + i]
-                zc *Kc = S + 3 * nn;
                 for (int t = threadIdx.x; t < n * (n - 1) / 2; t += blockDim.x) {
                     int i, j;
                     tri_index(t, n, i, j);
@@ -488,24 +536,24 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     Kc[j * n + i] = k10[i * n + j] - k10[j * n + i];
                 }
                 __syncthreads();
-                // ---- observables (18 complex partial sums)
+                // ---- observables (18 complex partial sums, FP64 accumulation)
                 double part[kNPart];
 #pragma unroll
                 for (int q = 0; q < kNPart; ++q) part[q] = 0.0;
                 for (int a = threadIdx.x; a < n; a += blockDim.x) {
-                    const zc d = rho[a * n + a];
+                    const zc d = A::to(rho[a * n + a]);
                     if (a < h) { part[0] += d.x; part[1] += d.y; }
                     else { part[2] += d.x; part[3] += d.y; }
                     part[8] = fma(p.obs.jj1[a], d.x, part[8]);
                     part[9] = fma(p.obs.jj1[a], d.y, part[9]);
                     const double jpa = p.obs.jp[a], jma = p.obs.jm[a], mza = p.obs.mz[a];
                     if (jpa != 0.0) {
-                        const zc r = rho[(a + 1) * n + a];
+                        const zc r = A::to(rho[(a + 1) * n + a]);
                         part[10] = fma(jpa, r.x, part[10]);
                         part[11] = fma(jpa, r.y, part[11]);
                     }
                     if (jma != 0.0) {
-                        const zc r = rho[(a - 1) * n + a];
+                        const zc r = A::to(rho[(a - 1) * n + a]);
                         part[12] = fma(jma, r.x, part[12]);
                         part[13] = fma(jma, r.y, part[13]);
                     }
@@ -513,7 +561,7 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     part[15] = fma(mza, d.y, part[15]);
                 }
                 for (int e = threadIdx.x; e < p.obs.n_t1b; e += blockDim.x) {
-                    const zc r = rho[p.obs.t1b_idx[e]];
+                    const zc r = A::to(rho[p.obs.t1b_idx[e]]);
                     part[4] = fma(p.obs.t1b_val[e], r.x, part[4]);
                     part[5] = fma(p.obs.t1b_val[e], r.y, part[5]);
                 }
@@ -521,50 +569,58 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     // PNAMP_Energy_OpenMP.f90:40-78:
                     // V[rho_ki rho_lj - rho_li rho_kj + d(rho_ik rho_jl - rho_jk rho_il)]
                     // + V/4 [K01_ij K10_kl + d K01_kl K10_ij],  K_xy = kappa_xy - kappa_yx
-                    zc e2 = mk(0, 0);
+                    const R quarter = A::real(0.25);
+                    Z e2 = zero;
                     for (int e = threadIdx.x; e < p.nrec; e += blockDim.x) {
                         const uint32_t pk = p.rec_idx[e];
                         const int i = pk & 0xff, j = (pk >> 8) & 0xff, k = (pk >> 16) & 0xff, l = pk >> 24;
-                        const double v = p.rec_v[e];
-                        zc t = rho[k * n + i] * rho[l * n + j];
+                        const R v = A::pick(p.rec_v, p.rec_vd, e);
+                        Z t = rho[k * n + i] * rho[l * n + j];
                         t = zfms(rho[l * n + i], rho[k * n + j], t);
-                        zc u = Kc[i * n + j] * Kc[l * n + k];
+                        Z u = Kc[i * n + j] * Kc[l * n + k];
                         if (i + j != k + l) {
                             t = zfma(rho[i * n + k], rho[j * n + l], t);
                             t = zfms(rho[j * n + k], rho[i * n + l], t);
                             u = zfma(Kc[k * n + l], Kc[j * n + i], u);
                         }
-                        t = rfma(0.25, u, t);
+                        t = rfma(quarter, u, t);
                         e2 = rfma(v, t, e2);
                     }
-                    part[6] += e2.x;
-                    part[7] += e2.y;
+                    const zc e2c = A::to(e2);
+                    part[6] += e2c.x;
+                    part[7] += e2c.y;
                 }
                 {   // <J^2> (ZJ2_0, PNAMP_ME2B.f90:45-147) summed over x, y, z with
                     // Jx, Jy = (J+ +- J-)/(2, 2i):  sum_a j(j+1) rho_aa [above]
                     // + Tr(J+ rho) Tr(J- rho) + Tr(Jz rho)^2 - Tr(J+ rho J- rho) - Tr(Jz rho Jz rho)
                     // + [Tr(J+ k10 J+ k01^T) + Tr(J- k10 J- k01^T)]/2 + Tr(Jz k10 Jz k01^T)
-                    zc rest = mk(0, 0);
+                    const R half = A::real(0.5);
+                    Z rest = zero;
                     for (int t = threadIdx.x; t < nn; t += blockDim.x) {
                         const int a = t / n, c = t % n;
-                        const double jpa = p.obs.jp[a], jma = p.obs.jm[a], jpc = p.obs.jp[c], jmc = p.obs.jm[c];
-                        const double mzz = p.obs.mz[a] * p.obs.mz[c];
-                        zc q = mzz * (k10[t] * k01[t]);
+                        const R jpa = A::pick(p.obs.jp, p.obs.jp_d, a), jma = A::pick(p.obs.jm, p.obs.jm_d, a);
+                        const R jpc = A::pick(p.obs.jp, p.obs.jp_d, c), jmc = A::pick(p.obs.jm, p.obs.jm_d, c);
+                        const R mzz = A::rmul(A::pick(p.obs.mz, p.obs.mz_d, a), A::pick(p.obs.mz, p.obs.mz_d, c));
+                        Z q = mzz * (k10[t] * k01[t]);
                         q = zfms(mzz * rho[t], rho[c * n + a], q);
-                        if (jpa != 0.0 && jmc != 0.0) q = zfms((jpa * jmc) * rho[(a + 1) * n + c], rho[(c - 1) * n + a], q);
-                        if (jpa != 0.0 && jpc != 0.0) q = zfma((0.5 * jpa * jpc) * k10[(a + 1) * n + c], k01[a * n + c + 1], q);
-                        if (jma != 0.0 && jmc != 0.0) q = zfma((0.5 * jma * jmc) * k10[(a - 1) * n + c], k01[a * n + c - 1], q);
+                        if (A::nz(jpa) && A::nz(jmc))
+                            q = zfms(A::rmul(jpa, jmc) * rho[(a + 1) * n + c], rho[(c - 1) * n + a], q);
+                        if (A::nz(jpa) && A::nz(jpc))
+                            q = zfma(A::rmul(half, A::rmul(jpa, jpc)) * k10[(a + 1) * n + c], k01[a * n + c + 1], q);
+                        if (A::nz(jma) && A::nz(jmc))
+                            q = zfma(A::rmul(half, A::rmul(jma, jmc)) * k10[(a - 1) * n + c], k01[a * n + c - 1], q);
                         rest = rest + q;
                     }
-                    part[8] += rest.x;
-                    part[9] += rest.y;
+                    const zc rc = A::to(rest);
+                    part[8] += rc.x;
+                    part[9] += rc.y;
                 }
                 if (p.iE2) {
 #pragma unroll
                     for (int q = 0; q < kNTrace; ++q) {
                         double sr = 0.0, si = 0.0;
                         for (int e = p.obs.q_off[q] + threadIdx.x; e < p.obs.q_off[q + 1]; e += blockDim.x) {
-                            const zc r = rho[p.obs.q_idx[e]];
+                            const zc r = A::to(rho[p.obs.q_idx[e]]);
                             sr = fma(p.obs.q_val[e], r.x, sr);
                             si = fma(p.obs.q_val[e], r.y, si);
                         }
@@ -616,17 +672,27 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
     }
 }
 
-cudaError_t point_blocks_per_sm(int smem_bytes, int *per_sm) {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, point_kernel, kThreads, smem_bytes);
+template <class Z>
+static const void *point_fn() {
+    return reinterpret_cast<const void *>(point_kernel<Z>);
 }
 
-cudaError_t set_point_smem(int bytes) {
-    return cudaFuncSetAttribute(point_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+cudaError_t point_blocks_per_sm(int form, int smem_bytes, int *per_sm) {
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        per_sm, form == 1 ? point_fn<zd>() : point_fn<zc>(), kThreads, smem_bytes);
+}
+
+cudaError_t set_point_smem(int form, int bytes) {
+    return cudaFuncSetAttribute(form == 1 ? point_fn<zd>() : point_fn<zc>(),
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc *scratch, int grid,
                           double *zres, int *status, cudaStream_t st) {
-    point_kernel<<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status);
+    if (p.form == 1)
+        point_kernel<zd><<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status);
+    else
+        point_kernel<zc><<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status);
     return cudaGetLastError();
 }
 

@@ -42,7 +42,8 @@ _lib = None
 # Every symbol the public header declares (tests check the library exports them).
 EXPORTS = ("pnamp_init", "pnamp_n_euler", "pnamp_pair", "pnamp_batch", "pnamp_batch_device",
            "pnamp_project", "pnamp_project_device", "pnamp_sync", "pnamp_free",
-           "pnamp_strerror", "pnamp_version", "pnamp_batch_device_noalloc")
+           "pnamp_strerror", "pnamp_version", "pnamp_batch_device_noalloc", "pnamp_set_form")
+FORMS = {"fp64": 0, "df64": 1}
 PNAMP_ERR_SCRATCH_LIMIT = 7
 
 
@@ -92,6 +93,7 @@ def load_library(path: str | None = None):
     vp = C.c_void_p
     lib.pnamp_init.argtypes = [C.POINTER(_Space), C.POINTER(_Ham), C.POINTER(_Mesh), C.POINTER(vp)]
     lib.pnamp_n_euler.argtypes = [vp]
+    lib.pnamp_set_form.argtypes = [vp, C.c_int]
     lib.pnamp_pair.argtypes = [vp] + [C.POINTER(C.c_double)] * 5 + [C.POINTER(C.c_int)]
     lib.pnamp_batch.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_int)]
@@ -127,7 +129,7 @@ class PnampContext:
     """A built PNAMP context: model space + Hamiltonian + mesh on the GPU."""
 
     def __init__(self, sp: ModelSpace, e0: float, t1b, recs, vbar, mesh: Mesh,
-                 q2=None, cscale: float = 1.0, iscale: int = 0):
+                 q2=None, cscale: float = 1.0, iscale: int = 0, form: str = "fp64"):
         lib = load_library()
         n = sp.nlev
         self.sp, self.mesh, self.n = sp, mesh, n
@@ -167,6 +169,14 @@ class PnampContext:
             raise PnampError(rc, "pnamp_init")
         self._h = h
         self.n_euler = lib.pnamp_n_euler(h)
+        self.set_form(form)
+
+    def set_form(self, form: str):
+        """Arithmetic of the per-point algebra: "fp64" (plain) or "df64" (double-float)."""
+        rc = load_library().pnamp_set_form(self._h, FORMS[form])
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_set_form")
+        self.form = form
 
     # ------------------------------------------------------------------
     def close(self):

@@ -20,8 +20,11 @@ NORM_TOL = 1e-10
 OBS_TOL = 1e-9
 
 
-def ctx_for(w, mesh, iE2=True):
-    return PnampContext(w.sp, w.e0, w.t1b, w.recs, w.vbar, mesh, q2=w.q2 if iE2 else None)
+FORMS = ["fp64", "df64"]
+
+
+def ctx_for(w, mesh, iE2=True, form="fp64"):
+    return PnampContext(w.sp, w.e0, w.t1b, w.recs, w.vbar, mesh, q2=w.q2 if iE2 else None, form=form)
 
 
 def oracle_zres(w, mesh, i, j, iE2=True):
@@ -53,28 +56,32 @@ def pf():
     return make_workload("pf", 2, Mesh(2, 3, 2, 3), seed=202)
 
 
-def test_sd_pair_matches_oracle(sd):
-    with ctx_for(sd, sd.mesh) as ctx:
+@pytest.mark.parametrize("form", FORMS)
+def test_sd_pair_matches_oracle(sd, form):
+    with ctx_for(sd, sd.mesh, form=form) as ctx:
         r = ctx.pair(*sd.vacua[0], *sd.vacua[1])
     assert (r.status & ~1).max() == 0
     assert_zres_close(r.zres, oracle_zres(sd, sd.mesh, 0, 1))
 
 
-def test_sd_diagonal_pair_matches_oracle(sd):
-    with ctx_for(sd, sd.mesh) as ctx:
+@pytest.mark.parametrize("form", FORMS)
+def test_sd_diagonal_pair_matches_oracle(sd, form):
+    with ctx_for(sd, sd.mesh, form=form) as ctx:
         z, st = ctx.batch([(*sd.vacua[1], *sd.vacua[1])])
     assert_zres_close(z[0], oracle_zres(sd, sd.mesh, 1, 1))
 
 
-def test_pf_pair_matches_oracle(pf):
-    with ctx_for(pf, pf.mesh) as ctx:
+@pytest.mark.parametrize("form", FORMS)
+def test_pf_pair_matches_oracle(pf, form):
+    with ctx_for(pf, pf.mesh, form=form) as ctx:
         r = ctx.pair(*pf.vacua[0], *pf.vacua[1])
     assert_zres_close(r.zres, oracle_zres(pf, pf.mesh, 0, 1))
 
 
-def test_sdpf_n64_global_workspace_matches_oracle():
+@pytest.mark.parametrize("form", FORMS)
+def test_sdpf_n64_global_workspace_matches_oracle(form):
     w = make_workload("sdpf", 2, Mesh(1, 2, 1, 2), seed=303)
-    with ctx_for(w, w.mesh) as ctx:
+    with ctx_for(w, w.mesh, form=form) as ctx:
         r = ctx.pair(*w.vacua[0], *w.vacua[1])
     assert_zres_close(r.zres, oracle_zres(w, w.mesh, 0, 1))
 
@@ -116,12 +123,13 @@ def test_singular_u_is_reported(sd):
     assert e.value.code == PNAMP_ERR_SINGULAR_U
 
 
-def test_ge76_kernel_files_through_gpu(ge76):
+@pytest.mark.parametrize("form", FORMS)
+def test_ge76_kernel_files_through_gpu(ge76, form):
     """All 16 intact Ge76 pairs in one batch reproduce the reference's kernel files."""
     g = ge76
     mesh = Mesh(1, g["nbet"], 1, g["nfom"], ncosbet=g["ncosbet"])
     idx = [(i, j) for i in range(4) for j in range(4)]
-    with PnampContext(g["sp"], g["e0"], g["t1b"], g["recs"], g["vbar"], mesh, q2=g["q2"]) as ctx:
+    with PnampContext(g["sp"], g["e0"], g["t1b"], g["recs"], g["vbar"], mesh, q2=g["q2"], form=form) as ctx:
         z, st = ctx.batch([(g["U"][i], g["V"][i], g["U"][j], g["V"][j]) for i, j in idx])
         for k, (i, j) in enumerate(idx):
             kern = ctx.project(z[k], chop=False)
