@@ -86,10 +86,12 @@ int plan_placement(Params &p, int smem_max) {
     int fixed = 0;
     pl.off_piv = fixed; fixed += align((n + 8) * 4);
     pl.off_inv = fixed; fixed += align(n * 16);
-    pl.off_red = fixed; fixed += align(40 * (kThreads / 32) * 8);
+    pl.off_red = fixed; fixed += align(40 * (kThreads / 32) * 8);  // 36 observable slots per warp
     pl.off_rot = fixed; fixed += align(p.rot_elems * 16);
-    pl.off_vec = fixed; fixed += align((N + kNobs) * 16);
-    const int bs = (int)(4 * nn * 16), bt = (int)(nn * 16), by = (int)(2 * nn * 16), buv = (int)(2 * nn * 8);
+    pl.off_vec = fixed; fixed += align((N + kNobs + 2 * p.nfom) * 16);  // + phase tables
+    // the Pfaffian matrix (N^2) shares storage with rho, kappa10, kappa01, K (4 n (n+1))
+    const long long s_elems = std::max<long long>((long long)N * N, 4LL * n * (n + 1));
+    const int bs = (int)(s_elems * 16), bt = (int)(nn * 16), by = (int)(2 * nn * 16), buv = (int)(2 * nn * 8);
     // greedy: keep the hottest arrays in shared memory
     int flags[4] = {1, 1, 1, 1};  // s, t, y, uv
     const int order[4] = {3, 2, 1, 0};  // spill uv first, then y, t, s
@@ -108,7 +110,7 @@ int plan_placement(Params &p, int smem_max) {
     pl.g_b = g; g += 2 * nn;
     pl.g_p = g; g += 4 * nn;
     pl.g_rw = g; g += nn;
-    pl.g_s = g; if (!pl.s_smem) g += 4 * nn;
+    pl.g_s = g; if (!pl.s_smem) g += s_elems;
     pl.g_t = g; if (!pl.t_smem) g += nn;
     pl.g_y = g; if (!pl.y_smem) g += 2 * nn;
     pl.g_uv = g; if (!pl.uv_smem) g += nn;  // 2 n^2 doubles = n^2 complex slots
@@ -217,6 +219,7 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
     }
     // mesh
     if (m->nalp < 1 || m->nbet < 1 || m->ngam < 1 || m->nfom < 1) return PNAMP_ERR_ARG;
+    if (m->nfom > 64) return PNAMP_ERR_UNSUPPORTED;
     if (m->ncosbet != 1 && m->ncosbet != 2) return PNAMP_ERR_ARG;
     if (!m->alpha || !m->beta || !m->gamma || !m->walp || !m->wbet || !m->wgam) return PNAMP_ERR_ARG;
     const int nbu = std::max(m->nbet / m->ncosbet, 1);
@@ -246,7 +249,7 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
         for (int c = 0; c < n; ++c) {  // sum_{a,c} rho(c,a) t(a,c)
             const double v = h->t1b[a + (size_t)c * n];
             if (v != 0.0) {
-                t1b_idx.push_back(c * n + a);
+                t1b_idx.push_back(c * 256 + a);  // row c, column a of rho
                 t1b_val.push_back(v);
             }
         }
@@ -262,7 +265,7 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
                     // ZQ2: Q(a,b) rho(b,a); ZQ2t: Q(b,a) rho(b,a), proton rows a
                     const double v = (q < 5) ? Q[a + (size_t)b * n] : Q[b + (size_t)a * n];
                     if (v != 0.0) {
-                        q_idx.push_back(b * n + a);
+                        q_idx.push_back(b * 256 + a);  // row b, column a of rho
                         q_val.push_back(v);
                     }
                 }

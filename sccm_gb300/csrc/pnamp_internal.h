@@ -13,7 +13,7 @@ constexpr int kJJMax = 6;
 constexpr int kNK = 2 * kJJMax + 1;
 constexpr int kMaxN = 64;
 constexpr int kMaxBlocks = 64;           // rotation blocks (t, n, l, j) of a model space
-constexpr int kThreads = 256;            // threads per CTA of the point kernel
+constexpr int kThreads = 512;            // threads per CTA of the point kernel (<= 128 registers)
 constexpr int kNTrace = 10;              // proton traces of Q_{2mu} rho and Q_{2mu}^dagger rho
 constexpr int kNJKK = 1 + 25 + 81 + 169; // (J, K1, K2) with even J <= 6
 constexpr int kProjFields = 5;           // njkk, hjkk, nn, zz, j2

@@ -85,7 +85,7 @@ template <> struct Ar<zd> {
 // Pivot row for column k (largest |re|+|im|, first on ties, as IZAMAX): warp 0
 // searches, the result is broadcast through sh[0] (row) and sh[1] (zero column).
 template <typename T>
-__device__ __forceinline__ int pivot_search(const T *A, int lda, int k, int n, int *sh, bool &zero) {
+__device__ __forceinline__ int pivot_search(const T *A, int lda, int k, int n, int *sh, T *invd, bool &zero) {
     if (threadIdx.x < 32) {
         double v = -1.0;
         int idx = 0x7fffffff;
@@ -108,8 +108,10 @@ __device__ __forceinline__ int pivot_search(const T *A, int lda, int k, int n, i
         if (threadIdx.x == 0) {
             // no comparable entry (all NaN): report a zero column, keep row k
             const bool none = (idx == 0x7fffffff);
+            const bool z = none || v == 0.0;
             sh[0] = none ? k : idx;
-            sh[1] = (none || v == 0.0) ? 1 : 0;
+            sh[1] = z ? 1 : 0;
+            invd[k] = z ? szero<T>() : srecip(A[(none ? k : idx) * lda + k]);
         }
     }
     __syncthreads();
@@ -125,7 +127,7 @@ __device__ bool lu_factor(T *A, int n, int lda, int *perm, T *invd, int *sh) {
     bool sing = false;
     for (int k = 0; k < n; ++k) {
         bool zero;
-        const int p = pivot_search(A, lda, k, n, sh, zero);
+        const int p = pivot_search(A, lda, k, n, sh, invd, zero);
         if (p != k)
             for (int j = threadIdx.x; j < n; j += blockDim.x) {
                 const T t = A[k * lda + j];
@@ -136,11 +138,9 @@ __device__ bool lu_factor(T *A, int n, int lda, int *perm, T *invd, int *sh) {
         __syncthreads();
         if (zero) {
             sing = true;
-            if (threadIdx.x == 0) invd[k] = szero<T>();
             continue;
         }
-        const T inv = srecip(A[k * lda + k]);
-        if (threadIdx.x == 0) invd[k] = inv;
+        const T inv = invd[k];
         for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[i * lda + k] = smul(A[i * lda + k], inv);
         __syncthreads();
         const int m = n - k - 1;
@@ -221,9 +221,9 @@ __device__ __forceinline__ void exch_upper(Z *S, int N, int r, int p, int q) {
 // |pivot| <= 1e-13, and the Schur complement is updated in place. The running
 // product is kept in FP64. `vec` holds N scratch values.
 template <class Z>
-__device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int &underflow) {
+__device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &underflow) {
     using A = Ar<Z>;
-    zc pf = mk(1.0, 0.0);
+    zc pf = mk(1.0, 0.0);  // running product, meaningful in thread 0
     underflow = 0;
     const int NB = N / 2;
     for (int k = 0; k < NB - 1; ++k) {
@@ -254,19 +254,23 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int &underflow) {
         if (i2 == c) phas = -phas;
         if (i1 != r) exch_upper(S, N, r, r, i1);
         if (i2 != c) exch_upper(S, N, r, c, i2);
-        const Z ssz = S[r * N + c];
-        const zc ss = A::to(ssz);
-        if (!zfinite(ss)) {
-            underflow = 2;
+        if (threadIdx.x == 0) {  // pivot test, reciprocal and running product by one thread
+            const Z ssz = S[r * N + c];
+            const zc ss = A::to(ssz);
+            const int f = !zfinite(ss) ? 2 : (!(abs2(ss) > 1.0e-26) ? 1 : 0);
+            flag[0] = f;
+            if (f == 0) {
+                vec[c] = zrecip(ssz);
+                pf = phas * (pf * ss);
+            }
+        }
+        __syncthreads();
+        if (flag[0]) {
+            underflow = flag[0];
             __syncthreads();
             return mk(0.0, 0.0);
         }
-        if (!(abs2(ss) > 1.0e-26)) {
-            underflow = 1;
-            __syncthreads();
-            return mk(0.0, 0.0);
-        }
-        const Z inv = zrecip(ssz);
+        const Z inv = vec[c];
         for (int i = c + 1 + threadIdx.x; i < N; i += blockDim.x) vec[i] = S[c * N + i] * inv;
         __syncthreads();
         const int mm = N - c - 1, TT = mm * (mm - 1) / 2;
@@ -280,10 +284,9 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int &underflow) {
             s = zfms(S[r * N + i], vec[j], s);
             S[i * N + j] = s;
         }
-        pf = phas * (pf * ss);
         __syncthreads();
     }
-    pf = pf * A::to(S[(N - 2) * N + N - 1]);
+    if (threadIdx.x == 0) pf = pf * A::to(S[(N - 2) * N + N - 1]);
     __syncthreads();
     return pf;
 }
@@ -357,7 +360,13 @@ cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *
 }
 
 // ------------------------------------------------------------------ points
-constexpr int kNPart = 36;  // 18 complex partial sums per gauge point
+constexpr int kNSlot = 36;  // 18 complex observable sums per gauge point (warp partials in shared)
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
 
 template <class Z>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -368,6 +377,8 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
     extern __shared__ __align__(16) unsigned char smem[];
     const int n = p.n, h = p.h, N = p.N2;
     const int nn = n * n;
+    const int ld = n + 1;  // density row stride: transposed reads stay bank-conflict free
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const Placement &pl = p.place;
     zc *slot = scratch + (long long)blockIdx.x * pl.slot_elems;
     Z *X = reinterpret_cast<Z *>(slot + pl.g_x);    // R W R^T
@@ -378,20 +389,28 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
     Z *S = reinterpret_cast<Z *>(pl.s_smem ? (void *)(smem + pl.off_s) : (void *)(slot + pl.g_s));
     Z *T = reinterpret_cast<Z *>(pl.t_smem ? (void *)(smem + pl.off_t) : (void *)(slot + pl.g_t));
     Z *Y = reinterpret_cast<Z *>(pl.y_smem ? (void *)(smem + pl.off_y) : (void *)(slot + pl.g_y));
-    R *V0s = reinterpret_cast<R *>(pl.uv_smem ? (void *)(smem + pl.off_uv) : (void *)(slot + pl.g_uv));
-    R *U0s = V0s + nn;
+    // V0^T and U0^T: V0t[k n + j] = V0(j, k)
+    R *V0t = reinterpret_cast<R *>(pl.uv_smem ? (void *)(smem + pl.off_uv) : (void *)(slot + pl.g_uv));
+    R *U0t = V0t + nn;
     int *perm = reinterpret_cast<int *>(smem + pl.off_piv);
     int *sh = perm + n;
     Z *invd = reinterpret_cast<Z *>(smem + pl.off_inv);
     double *red = reinterpret_cast<double *>(smem + pl.off_red);
     zc *rot = reinterpret_cast<zc *>(smem + pl.off_rot);
     Z *vec = reinterpret_cast<Z *>(smem + pl.off_vec);
-    zc *acc = reinterpret_cast<zc *>(vec + N);  // kNobs accumulators
-    Z *rho = S, *k10 = S + nn, *k01 = S + 2 * nn;
-    Z *Kc = S + 3 * nn;  // antisymmetrised pairing tensors
+    zc *acc = reinterpret_cast<zc *>(vec + N);      // kNobs accumulators (thread 0)
+    zc *eph = acc + kNobs;                          // e^{i phi_l}, l < NFOM
+    Z *ephz = reinterpret_cast<Z *>(eph + p.nfom);  // the same in the point arithmetic
+    Z *rho = S, *k10 = S + n * ld, *k01 = S + 2 * n * ld;
+    Z *Kc = S + 3 * n * ld;  // antisymmetrised pairing tensors
 
-    const long long total = (long long)npairs * p.n_euler;
     const double twopi = 6.283185307179586476925287;
+    for (int l = threadIdx.x; l < p.nfom; l += blockDim.x) {
+        const zc e = expi(p.nfom == 1 ? 0.0 : twopi * l / p.nfom);
+        eph[l] = e;
+        ephz[l] = A::from(e);
+    }
+    const long long total = (long long)npairs * p.n_euler;
     int cur_pair = -1;
     for (long long item = blockIdx.x; item < total; item += gridDim.x) {
         const int pair = (int)(item / p.n_euler), ie = (int)(item % p.n_euler);
@@ -412,8 +431,9 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
         if (pair != cur_pair) {
             __syncthreads();
             for (int t = threadIdx.x; t < nn; t += blockDim.x) {
-                V0s[t] = A::real(gV0[t]);
-                U0s[t] = A::real(gU0[t]);
+                const int k = t / n, j = t % n;
+                V0t[t] = A::real(gV0[j * n + k]);
+                U0t[t] = A::real(gU0[j * n + k]);
             }
             cur_pair = pair;
         }
@@ -477,16 +497,14 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
         __syncthreads();
 
         int flags = 0;
+        const Z zero = A::from(mk(0.0, 0.0));
+        const Z csz = A::from(mk(p.cscale, 0.0)), mcs = A::from(mk(-p.cscale, 0.0));
         for (int lp = 0; lp < p.nfom; ++lp) {
-            const double php = (p.nfom == 1) ? 0.0 : twopi * lp / p.nfom;
-            const zc ep = expi(php);
+            const Z zep = ephz[lp], zepc = zconj(zep);
             for (int ln = 0; ln < p.nfom; ++ln) {
-                const double phn = (p.nfom == 1) ? 0.0 : twopi * ln / p.nfom;
-                const zc en = expi(phn);
+                const Z zen = ephz[ln], zenc = zconj(zen);
                 // ---- S = Cscale [[D X D, -I], [I, -Z0]] (upper triangle)
-                const double cs = p.cscale;
-                const Z dpp = A::from(cs * (ep * ep)), dpn = A::from(cs * (ep * en)), dnn = A::from(cs * (en * en));
-                const Z mcs = A::from(mk(-cs, 0.0)), zero = A::from(mk(0.0, 0.0));
+                const Z dpp = csz * (zep * zep), dpn = csz * (zep * zen), dnn = csz * (zen * zen);
                 for (int t = threadIdx.x; t < N * (N - 1) / 2; t += blockDim.x) {
                     int i, j;
                     tri_index(t, N, i, j);
@@ -497,15 +515,14 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     } else if (i < n) {
                         v = (j - n == i) ? mcs : zero;
                     } else {
-                        v = A::from(mk(-cs * gZ0[(i - n) * n + (j - n)], 0.0));
+                        v = A::from(mk(-p.cscale * gZ0[(i - n) * n + (j - n)], 0.0));
                     }
                     S[i * N + j] = v;
                 }
                 __syncthreads();
                 int under;
-                const zc pf = pfaffian_upper<Z>(S, N, vec, red, under);
+                const zc pf = pfaffian_upper<Z>(S, N, vec, red, sh + 2, under);
                 // ---- T22(phi) and right-hand sides
-                const Z zep = A::from(ep), zen = A::from(en), zepc = A::from(zconj(ep)), zenc = A::from(zconj(en));
                 for (int t = threadIdx.x; t < nn; t += blockDim.x) {
                     Z s = zep * P[t];
                     s = zfma(zen, P[nn + t], s);
@@ -517,53 +534,62 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                 __syncthreads();
                 const bool sing = lu_factor<Z>(T, n, n, perm, invd, sh);
                 row_solve<Z>(Y, 2 * n, n, T, n, n, perm, invd);
-                // ---- densities into the Pfaffian's storage
+                // ---- densities into the Pfaffian's storage, row stride ld
                 for (int t = threadIdx.x; t < 3 * nn; t += blockDim.x) {
                     const int q = t / nn, e = t % nn, i = e / n, j = e % n;
                     const Z *Yr = (q == 2) ? Y + (n + i) * n : Y + i * n;
-                    const R *M = (q == 1) ? U0s + j * n : V0s + j * n;
+                    const R *M = (q == 1) ? U0t + j : V0t + j;
                     Z s = zero;
-                    for (int k = 0; k < n; ++k) s = rfma(M[k], Yr[k], s);
+                    for (int k = 0; k < n; ++k) s = rfma(M[k * n], Yr[k], s);
                     const Z di = (i < h) ? zep : zen;
-                    S[t] = (q == 2) ? -(zconj(di) * s) : di * s;
+                    S[q * n * ld + i * ld + j] = (q == 2) ? -(zconj(di) * s) : di * s;
                 }
                 __syncthreads();
-                // K01_ij (i < j) at Kc[i n + j], K10_ij at Kc[j n + i]
+                // K01_ij (i < j) at Kc[i ld + j], K10_ij at Kc[j ld + i]
                 for (int t = threadIdx.x; t < n * (n - 1) / 2; t += blockDim.x) {
                     int i, j;
                     tri_index(t, n, i, j);
-                    Kc[i * n + j] = k01[i * n + j] - k01[j * n + i];
-                    Kc[j * n + i] = k10[i * n + j] - k10[j * n + i];
+                    Kc[i * ld + j] = k01[i * ld + j] - k01[j * ld + i];
+                    Kc[j * ld + i] = k10[i * ld + j] - k10[j * ld + i];
                 }
                 __syncthreads();
-                // ---- observables (18 complex partial sums, FP64 accumulation)
-                double part[kNPart];
-#pragma unroll
-                for (int q = 0; q < kNPart; ++q) part[q] = 0.0;
-                for (int a = threadIdx.x; a < n; a += blockDim.x) {
-                    const zc d = A::to(rho[a * n + a]);
-                    if (a < h) { part[0] += d.x; part[1] += d.y; }
-                    else { part[2] += d.x; part[3] += d.y; }
-                    part[8] = fma(p.obs.jj1[a], d.x, part[8]);
-                    part[9] = fma(p.obs.jj1[a], d.y, part[9]);
-                    const double jpa = p.obs.jp[a], jma = p.obs.jm[a], mza = p.obs.mz[a];
-                    if (jpa != 0.0) {
-                        const zc r = A::to(rho[(a + 1) * n + a]);
-                        part[10] = fma(jpa, r.x, part[10]);
-                        part[11] = fma(jpa, r.y, part[11]);
+                // ---- observables: each sum is warp-reduced at once into red[slot][warp]
+                auto put = [&](int slot, double v) {
+                    v = warp_sum(v);
+                    if (lane == 0) red[slot * nw + wid] = v;
+                };
+                {
+                    double z0 = 0, z1 = 0, n0 = 0, n1 = 0, j0 = 0, j1 = 0, p0 = 0, p1 = 0, m0 = 0, m1 = 0, c0 = 0,
+                           c1 = 0, t0 = 0, t1 = 0;
+                    for (int a = threadIdx.x; a < n; a += blockDim.x) {
+                        const zc d = A::to(rho[a * ld + a]);
+                        if (a < h) { z0 += d.x; z1 += d.y; }
+                        else { n0 += d.x; n1 += d.y; }
+                        j0 = fma(p.obs.jj1[a], d.x, j0);
+                        j1 = fma(p.obs.jj1[a], d.y, j1);
+                        const double jpa = p.obs.jp[a], jma = p.obs.jm[a], mza = p.obs.mz[a];
+                        if (jpa != 0.0) {
+                            const zc r = A::to(rho[(a + 1) * ld + a]);
+                            p0 = fma(jpa, r.x, p0);
+                            p1 = fma(jpa, r.y, p1);
+                        }
+                        if (jma != 0.0) {
+                            const zc r = A::to(rho[(a - 1) * ld + a]);
+                            m0 = fma(jma, r.x, m0);
+                            m1 = fma(jma, r.y, m1);
+                        }
+                        c0 = fma(mza, d.x, c0);
+                        c1 = fma(mza, d.y, c1);
                     }
-                    if (jma != 0.0) {
-                        const zc r = A::to(rho[(a - 1) * n + a]);
-                        part[12] = fma(jma, r.x, part[12]);
-                        part[13] = fma(jma, r.y, part[13]);
+                    for (int e = threadIdx.x; e < p.obs.n_t1b; e += blockDim.x) {
+                        const int ix = p.obs.t1b_idx[e];
+                        const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
+                        t0 = fma(p.obs.t1b_val[e], r.x, t0);
+                        t1 = fma(p.obs.t1b_val[e], r.y, t1);
                     }
-                    part[14] = fma(mza, d.x, part[14]);
-                    part[15] = fma(mza, d.y, part[15]);
-                }
-                for (int e = threadIdx.x; e < p.obs.n_t1b; e += blockDim.x) {
-                    const zc r = A::to(rho[p.obs.t1b_idx[e]]);
-                    part[4] = fma(p.obs.t1b_val[e], r.x, part[4]);
-                    part[5] = fma(p.obs.t1b_val[e], r.y, part[5]);
+                    put(0, z0); put(1, z1); put(2, n0); put(3, n1); put(4, t0); put(5, t1);
+                    put(10, p0); put(11, p1); put(12, m0); put(13, m1); put(14, c0); put(15, c1);
+                    put(16, j0); put(17, j1);
                 }
                 {   // two-body energy, exact regrouping of the 8-term sum of
                     // PNAMP_Energy_OpenMP.f90:40-78:
@@ -571,24 +597,33 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     // + V/4 [K01_ij K10_kl + d K01_kl K10_ij],  K_xy = kappa_xy - kappa_yx
                     const R quarter = A::real(0.25);
                     Z e2 = zero;
-                    for (int e = threadIdx.x; e < p.nrec; e += blockDim.x) {
-                        const uint32_t pk = p.rec_idx[e];
+                    auto rec = [&](uint32_t pk, R v) {
                         const int i = pk & 0xff, j = (pk >> 8) & 0xff, k = (pk >> 16) & 0xff, l = pk >> 24;
-                        const R v = A::pick(p.rec_v, p.rec_vd, e);
-                        Z t = rho[k * n + i] * rho[l * n + j];
-                        t = zfms(rho[l * n + i], rho[k * n + j], t);
-                        Z u = Kc[i * n + j] * Kc[l * n + k];
+                        Z t = rho[k * ld + i] * rho[l * ld + j];
+                        t = zfms(rho[l * ld + i], rho[k * ld + j], t);
+                        Z u = Kc[i * ld + j] * Kc[l * ld + k];
                         if (i + j != k + l) {
-                            t = zfma(rho[i * n + k], rho[j * n + l], t);
-                            t = zfms(rho[j * n + k], rho[i * n + l], t);
-                            u = zfma(Kc[k * n + l], Kc[j * n + i], u);
+                            t = zfma(rho[i * ld + k], rho[j * ld + l], t);
+                            t = zfms(rho[j * ld + k], rho[i * ld + l], t);
+                            u = zfma(Kc[k * ld + l], Kc[j * ld + i], u);
                         }
                         t = rfma(quarter, u, t);
                         e2 = rfma(v, t, e2);
+                    };
+                    const int stride = blockDim.x;
+                    for (int e = threadIdx.x; e < p.nrec; e += 2 * stride) {
+                        const int e1 = e + stride;
+                        const uint32_t pk0 = p.rec_idx[e];
+                        const R v0 = A::pick(p.rec_v, p.rec_vd, e);
+                        const bool two = e1 < p.nrec;
+                        const uint32_t pk1 = two ? p.rec_idx[e1] : 0u;
+                        const R v1 = two ? A::pick(p.rec_v, p.rec_vd, e1) : A::real(0.0);
+                        rec(pk0, v0);
+                        if (two) rec(pk1, v1);
                     }
                     const zc e2c = A::to(e2);
-                    part[6] += e2c.x;
-                    part[7] += e2c.y;
+                    put(6, e2c.x);
+                    put(7, e2c.y);
                 }
                 {   // <J^2> (ZJ2_0, PNAMP_ME2B.f90:45-147) summed over x, y, z with
                     // Jx, Jy = (J+ +- J-)/(2, 2i):  sum_a j(j+1) rho_aa [above]
@@ -601,60 +636,65 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                         const R jpa = A::pick(p.obs.jp, p.obs.jp_d, a), jma = A::pick(p.obs.jm, p.obs.jm_d, a);
                         const R jpc = A::pick(p.obs.jp, p.obs.jp_d, c), jmc = A::pick(p.obs.jm, p.obs.jm_d, c);
                         const R mzz = A::rmul(A::pick(p.obs.mz, p.obs.mz_d, a), A::pick(p.obs.mz, p.obs.mz_d, c));
-                        Z q = mzz * (k10[t] * k01[t]);
-                        q = zfms(mzz * rho[t], rho[c * n + a], q);
+                        const int ac = a * ld + c;
+                        Z q = mzz * (k10[ac] * k01[ac]);
+                        q = zfms(mzz * rho[ac], rho[c * ld + a], q);
                         if (A::nz(jpa) && A::nz(jmc))
-                            q = zfms(A::rmul(jpa, jmc) * rho[(a + 1) * n + c], rho[(c - 1) * n + a], q);
+                            q = zfms(A::rmul(jpa, jmc) * rho[ac + ld], rho[(c - 1) * ld + a], q);
                         if (A::nz(jpa) && A::nz(jpc))
-                            q = zfma(A::rmul(half, A::rmul(jpa, jpc)) * k10[(a + 1) * n + c], k01[a * n + c + 1], q);
+                            q = zfma(A::rmul(half, A::rmul(jpa, jpc)) * k10[ac + ld], k01[ac + 1], q);
                         if (A::nz(jma) && A::nz(jmc))
-                            q = zfma(A::rmul(half, A::rmul(jma, jmc)) * k10[(a - 1) * n + c], k01[a * n + c - 1], q);
+                            q = zfma(A::rmul(half, A::rmul(jma, jmc)) * k10[ac - ld], k01[ac - 1], q);
                         rest = rest + q;
                     }
                     const zc rc = A::to(rest);
-                    part[8] += rc.x;
-                    part[9] += rc.y;
+                    put(8, rc.x);
+                    put(9, rc.y);
                 }
                 if (p.iE2) {
-#pragma unroll
                     for (int q = 0; q < kNTrace; ++q) {
                         double sr = 0.0, si = 0.0;
                         for (int e = p.obs.q_off[q] + threadIdx.x; e < p.obs.q_off[q + 1]; e += blockDim.x) {
-                            const zc r = A::to(rho[p.obs.q_idx[e]]);
+                            const int ix = p.obs.q_idx[e];
+                            const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
                             sr = fma(p.obs.q_val[e], r.x, sr);
                             si = fma(p.obs.q_val[e], r.y, si);
                         }
-                        part[16 + 2 * q] += sr;
-                        part[17 + 2 * q] += si;
+                        put(18 + 2 * q, sr);
+                        put(19 + 2 * q, si);
                     }
                 }
-                block_sum<kNPart>(part, red);
+                __syncthreads();
                 if (threadIdx.x == 0) {
-                    const zc zph = expi(-(php * p.nprot + phn * p.nneut));
+                    auto get = [&](int slot) {
+                        double v = 0.0;
+                        for (int w = 0; w < nw; ++w) v += red[slot * nw + w];
+                        return v;
+                    };
+                    const zc zph = expi(-(twopi * lp / p.nfom * p.nprot + twopi * ln / p.nfom * p.nneut));
                     const zc norm = (p.vacfac * det0 * det1) * (pf * zph);
-                    const zc zp = mk(part[0], part[1]), zn = mk(part[2], part[3]);
-                    const zc ekin = mk(part[4], part[5]), e2 = mk(part[6], part[7]);
-                    const zc trp = mk(part[10], part[11]), trm = mk(part[12], part[13]),
-                             trz = mk(part[14], part[15]);
-                    const zc j2 = mk(part[8], part[9]) + trp * trm + trz * trz;
+                    const zc trp = mk(get(10), get(11)), trm = mk(get(12), get(13)), trz = mk(get(14), get(15));
+                    const zc j2 = mk(get(16) + get(8), get(17) + get(9)) + trp * trm + trz * trz;
+                    const zc ekin = mk(get(4), get(5));
                     acc[0] = acc[0] + norm;
                     int f = (under == 1) ? 1 : (under == 2 ? 4 : 0);
                     if (sing) {
                         f |= 2;
                     } else {
-                        acc[1] = zfma(norm, zp, acc[1]);
-                        acc[2] = zfma(norm, zn, acc[2]);
+                        acc[1] = zfma(norm, mk(get(0), get(1)), acc[1]);
+                        acc[2] = zfma(norm, mk(get(2), get(3)), acc[2]);
                         acc[3] = zfma(norm, ekin, acc[3]);
-                        acc[6] = zfma(norm, ekin + e2 + mk(p.e0, 0.0), acc[6]);
+                        acc[6] = zfma(norm, ekin + mk(get(6), get(7)) + mk(p.e0, 0.0), acc[6]);
                         acc[7] = zfma(norm, j2, acc[7]);
                         if (p.iE2)
                             for (int q = 0; q < 5; ++q) {
-                                acc[8 + q] = zfma(norm, mk(part[16 + 2 * q], part[17 + 2 * q]), acc[8 + q]);
-                                acc[13 + q] = zfma(norm, mk(part[26 + 2 * q], part[27 + 2 * q]), acc[13 + q]);
+                                acc[8 + q] = zfma(norm, mk(get(18 + 2 * q), get(19 + 2 * q)), acc[8 + q]);
+                                acc[13 + q] = zfma(norm, mk(get(28 + 2 * q), get(29 + 2 * q)), acc[13 + q]);
                             }
                     }
                     flags |= f;
                 }
+                __syncthreads();
             }
         }
         if (threadIdx.x == 0) {
