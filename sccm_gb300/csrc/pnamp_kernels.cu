@@ -144,9 +144,18 @@ __device__ bool lu_factor(T *A, int n, int lda, int *perm, T *invd, int *sh) {
         for (int i = k + 1 + threadIdx.x; i < n; i += blockDim.x) A[i * lda + k] = smul(A[i * lda + k], inv);
         __syncthreads();
         const int m = n - k - 1;
-        for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
-            const int i = k + 1 + t / m, j = k + 1 + t % m;
-            A[i * lda + j] = sfms(A[i * lda + k], A[k * lda + j], A[i * lda + j]);
+        if (m > 0) {
+            const int dq = blockDim.x / m, dr = blockDim.x % m;
+            int i = k + 1 + threadIdx.x / m, j = k + 1 + threadIdx.x % m;
+            for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+                A[i * lda + j] = sfms(A[i * lda + k], A[k * lda + j], A[i * lda + j]);
+                i += dq;
+                j += dr;
+                if (j >= k + 1 + m) {
+                    j -= m;
+                    ++i;
+                }
+            }
         }
         __syncthreads();
     }
@@ -163,17 +172,31 @@ __device__ void row_solve(T *Y, int nr, int ldy, const T *A, int n, int lda, con
         __syncthreads();
         const int m = n - j - 1;
         if (m > 0) {
+            const int dq = blockDim.x / m, dr = blockDim.x % m;
+            int r = threadIdx.x / m, c = j + 1 + threadIdx.x % m;
             for (int t = threadIdx.x; t < nr * m; t += blockDim.x) {
-                const int r = t / m, c = j + 1 + t % m;
                 Y[r * ldy + c] = sfms(Y[r * ldy + j], A[j * lda + c], Y[r * ldy + c]);
+                r += dq;
+                c += dr;
+                if (c >= n) {
+                    c -= m;
+                    ++r;
+                }
             }
             __syncthreads();
         }
     }
     for (int j = n - 1; j > 0; --j) {  // Y2 L = Z, last column first
+        const int dq = blockDim.x / j, dr = blockDim.x % j;
+        int r = threadIdx.x / j, c = threadIdx.x % j;
         for (int t = threadIdx.x; t < nr * j; t += blockDim.x) {
-            const int r = t / j, c = t % j;
             Y[r * ldy + c] = sfms(Y[r * ldy + j], A[j * lda + c], Y[r * ldy + c]);
+            r += dq;
+            c += dr;
+            if (c >= j) {
+                c -= j;
+                ++r;
+            }
         }
         __syncthreads();
     }
@@ -360,7 +383,8 @@ cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *
 }
 
 // ------------------------------------------------------------------ points
-constexpr int kNSlot = 36;  // 18 complex observable sums per gauge point (warp partials in shared)
+constexpr int kNSlot = 36;  // observable sums: slots 0..37 final values, then per-warp partials
+static_assert(kThreads >= 32 * (kNTrace + 1), "one warp per Q trace plus warp 0");
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -535,14 +559,28 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                 const bool sing = lu_factor<Z>(T, n, n, perm, invd, sh);
                 row_solve<Z>(Y, 2 * n, n, T, n, n, perm, invd);
                 // ---- densities into the Pfaffian's storage, row stride ld
-                for (int t = threadIdx.x; t < 3 * nn; t += blockDim.x) {
-                    const int q = t / nn, e = t % nn, i = e / n, j = e % n;
-                    const Z *Yr = (q == 2) ? Y + (n + i) * n : Y + i * n;
-                    const R *M = (q == 1) ? U0t + j : V0t + j;
-                    Z s = zero;
-                    for (int k = 0; k < n; ++k) s = rfma(M[k * n], Yr[k], s);
-                    const Z di = (i < h) ? zep : zen;
-                    S[q * n * ld + i * ld + j] = (q == 2) ? -(zconj(di) * s) : di * s;
+                {
+                    const int dq = blockDim.x / n, dr = blockDim.x % n;
+                    for (int q = 0; q < 3; ++q) {
+                        const R *Mq = (q == 1) ? U0t : V0t;
+                        const Z *Yq = (q == 2) ? Y + nn : Y;
+                        Z *Sq = S + q * n * ld;
+                        int i = threadIdx.x / n, j = threadIdx.x % n;
+                        for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+                            const Z *Yr = Yq + i * n;
+                            const R *M = Mq + j;
+                            Z s = zero;
+                            for (int k = 0; k < n; ++k) s = rfma(M[k * n], Yr[k], s);
+                            const Z di = (i < h) ? zep : zen;
+                            Sq[i * ld + j] = (q == 2) ? -(zconj(di) * s) : di * s;
+                            i += dq;
+                            j += dr;
+                            if (j >= n) {
+                                j -= n;
+                                ++i;
+                            }
+                        }
+                    }
                 }
                 __syncthreads();
                 // K01_ij (i < j) at Kc[i ld + j], K10_ij at Kc[j ld + i]
@@ -553,15 +591,13 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     Kc[j * ld + i] = k10[i * ld + j] - k10[j * ld + i];
                 }
                 __syncthreads();
-                // ---- observables: each sum is warp-reduced at once into red[slot][warp]
-                auto put = [&](int slot, double v) {
-                    v = warp_sum(v);
-                    if (lane == 0) red[slot * nw + wid] = v;
-                };
-                {
+                // ---- observables. Final sums land in red[0..kNSlot); the energy and <J^2>
+                // sums, spread over all warps, leave per-warp partials in red[kNSlot + ..].
+                double *fin = red, *pw = red + kNSlot + 2;
+                if (wid == 0) {  // traces of rho: warp 0 alone
                     double z0 = 0, z1 = 0, n0 = 0, n1 = 0, j0 = 0, j1 = 0, p0 = 0, p1 = 0, m0 = 0, m1 = 0, c0 = 0,
                            c1 = 0, t0 = 0, t1 = 0;
-                    for (int a = threadIdx.x; a < n; a += blockDim.x) {
+                    for (int a = lane; a < n; a += 32) {
                         const zc d = A::to(rho[a * ld + a]);
                         if (a < h) { z0 += d.x; z1 += d.y; }
                         else { n0 += d.x; n1 += d.y; }
@@ -581,16 +617,39 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                         c0 = fma(mza, d.x, c0);
                         c1 = fma(mza, d.y, c1);
                     }
-                    for (int e = threadIdx.x; e < p.obs.n_t1b; e += blockDim.x) {
+                    for (int e = lane; e < p.obs.n_t1b; e += 32) {
                         const int ix = p.obs.t1b_idx[e];
                         const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
                         t0 = fma(p.obs.t1b_val[e], r.x, t0);
                         t1 = fma(p.obs.t1b_val[e], r.y, t1);
                     }
-                    put(0, z0); put(1, z1); put(2, n0); put(3, n1); put(4, t0); put(5, t1);
-                    put(10, p0); put(11, p1); put(12, m0); put(13, m1); put(14, c0); put(15, c1);
-                    put(16, j0); put(17, j1);
+                    const double vals[14] = {z0, z1, n0, n1, t0, t1, p0, p1, m0, m1, c0, c1, j0, j1};
+                    const int slots[14] = {0, 1, 2, 3, 4, 5, 10, 11, 12, 13, 14, 15, 16, 17};
+#pragma unroll
+                    for (int q = 0; q < 14; ++q) {
+                        const double v = warp_sum(vals[q]);
+                        if (lane == 0) fin[slots[q]] = v;
+                    }
+                } else if (p.iE2 && wid <= kNTrace) {  // Q_{2mu} traces: one warp per trace
+                    const int q = wid - 1;
+                    double sr = 0.0, si = 0.0;
+                    for (int e = p.obs.q_off[q] + lane; e < p.obs.q_off[q + 1]; e += 32) {
+                        const int ix = p.obs.q_idx[e];
+                        const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
+                        sr = fma(p.obs.q_val[e], r.x, sr);
+                        si = fma(p.obs.q_val[e], r.y, si);
+                    }
+                    sr = warp_sum(sr);
+                    si = warp_sum(si);
+                    if (lane == 0) {
+                        fin[18 + 2 * q] = sr;
+                        fin[19 + 2 * q] = si;
+                    }
                 }
+                auto put = [&](int slot, double v) {  // slot 0..3: energy re/im, <J^2> re/im
+                    v = warp_sum(v);
+                    if (lane == 0) pw[slot * nw + wid] = v;
+                };
                 {   // two-body energy, exact regrouping of the 8-term sum of
                     // PNAMP_Energy_OpenMP.f90:40-78:
                     // V[rho_ki rho_lj - rho_li rho_kj + d(rho_ik rho_jl - rho_jk rho_il)]
@@ -622,8 +681,8 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                         if (two) rec(pk1, v1);
                     }
                     const zc e2c = A::to(e2);
-                    put(6, e2c.x);
-                    put(7, e2c.y);
+                    put(0, e2c.x);
+                    put(1, e2c.y);
                 }
                 {   // <J^2> (ZJ2_0, PNAMP_ME2B.f90:45-147) summed over x, y, z with
                     // Jx, Jy = (J+ +- J-)/(2, 2i):  sum_a j(j+1) rho_aa [above]
@@ -631,8 +690,13 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     // + [Tr(J+ k10 J+ k01^T) + Tr(J- k10 J- k01^T)]/2 + Tr(Jz k10 Jz k01^T)
                     const R half = A::real(0.5);
                     Z rest = zero;
-                    for (int t = threadIdx.x; t < nn; t += blockDim.x) {
-                        const int a = t / n, c = t % n;
+                    const int dq = blockDim.x / n, dr = blockDim.x % n;
+                    int a = threadIdx.x / n, c = threadIdx.x % n;
+                    for (int t = threadIdx.x; t < nn; t += blockDim.x, a += dq, c += dr) {
+                        if (c >= n) {
+                            c -= n;
+                            ++a;
+                        }
                         const R jpa = A::pick(p.obs.jp, p.obs.jp_d, a), jma = A::pick(p.obs.jm, p.obs.jm_d, a);
                         const R jpc = A::pick(p.obs.jp, p.obs.jp_d, c), jmc = A::pick(p.obs.jm, p.obs.jm_d, c);
                         const R mzz = A::rmul(A::pick(p.obs.mz, p.obs.mz_d, a), A::pick(p.obs.mz, p.obs.mz_d, c));
@@ -648,28 +712,18 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                         rest = rest + q;
                     }
                     const zc rc = A::to(rest);
-                    put(8, rc.x);
-                    put(9, rc.y);
-                }
-                if (p.iE2) {
-                    for (int q = 0; q < kNTrace; ++q) {
-                        double sr = 0.0, si = 0.0;
-                        for (int e = p.obs.q_off[q] + threadIdx.x; e < p.obs.q_off[q + 1]; e += blockDim.x) {
-                            const int ix = p.obs.q_idx[e];
-                            const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
-                            sr = fma(p.obs.q_val[e], r.x, sr);
-                            si = fma(p.obs.q_val[e], r.y, si);
-                        }
-                        put(18 + 2 * q, sr);
-                        put(19 + 2 * q, si);
-                    }
+                    put(2, rc.x);
+                    put(3, rc.y);
                 }
                 __syncthreads();
                 if (threadIdx.x == 0) {
                     auto get = [&](int slot) {
-                        double v = 0.0;
-                        for (int w = 0; w < nw; ++w) v += red[slot * nw + w];
-                        return v;
+                        if (slot >= 6 && slot <= 9) {  // summed over warps
+                            double v = 0.0;
+                            for (int w = 0; w < nw; ++w) v += pw[(slot - 6) * nw + w];
+                            return v;
+                        }
+                        return fin[slot];
                     };
                     const zc zph = expi(-(twopi * lp / p.nfom * p.nprot + twopi * ln / p.nfom * p.nneut));
                     const zc norm = (p.vacfac * det0 * det1) * (pf * zph);
