@@ -257,8 +257,8 @@ def kernel_triaxial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1
                     cscale=1.0, iscale=0, iE2=True, euler_subset=None, point_log=None):
     """Kernel4Triaxial mesh loop (PNAMP_Kernel3D.f90:70-407) -> ZRES[P_E, NOBS].
 
-    Shell-model runs always take the Pfaffian branch (ide forced to 1,
-    Kernel3D.f90:140-159). `euler_subset` restricts the loop to a list of Euler
+    Shell-model runs take the Pfaffian branch (ide forced to 1, Kernel3D.f90:140-159)
+    unless NFOM = 1, where the Onishi formula gives the norm (Kernel3D.f90:286-290). `euler_subset` restricts the loop to a list of Euler
     indices (rows of ZRES left zero elsewhere) so tests can sample large meshes.
     """
     n = sp.nlev
@@ -284,8 +284,11 @@ def kernel_triaxial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1
                 zph_n = np.exp(-1j * phn * sp.nneut)
                 A = gauge_matrix(R, php, phn)
                 ub, vb = uvphiomega(A, U1, V1)
-                pf, st = pfaf_over(zzc0, ub, vb, cscale)
-                znorm = snpfaf * zdv0 * zdv1 * pf * zph_p * zph_n
+                if nf == 1:   # Kernel3D.f90:286-290: no number projection -> Onishi
+                    pf = znorm = onishi(U0, V0, ub, vb)
+                else:
+                    pf, st = pfaf_over(zzc0, ub, vb, cscale)
+                    znorm = snpfaf * zdv0 * zdv1 * pf * zph_p * zph_n
                 o = point_observables(sp, ham, A, U0, V0, U1, V1, znorm, iE2)
                 if point_log is not None:
                     point_log.append((ie, php, phn, pf, o))

@@ -478,25 +478,29 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
             for (int io = 0; io < kNobs; ++io) acc[io] = mk(0.0, 0.0);
         }
         __syncthreads();
-        // ---- R W, R V1, conj(R) U1 (FP64)
+        // ---- R W (or, for the Onishi norm, R U1 and conj(R) V1), R V1, conj(R) U1 (FP64)
+        const bool onishi = (p.nfom == 1);
+        zc *Xz = reinterpret_cast<zc *>(X);
         for (int t = threadIdx.x; t < nn; t += blockDim.x) {
             const int a = t / n, j = t % n;
             const int b = p.row_blk[a], s0 = p.blk_start[b], d = p.blk_size[b];
             const zc *Rr = rot + p.blk_roff[b] + (a - s0) * d;
-            zc rw = mk(0, 0), b1 = mk(0, 0), b2 = mk(0, 0);
+            zc rw = mk(0, 0), b1 = mk(0, 0), b2 = mk(0, 0), cv = mk(0, 0);
             for (int k = 0; k < d; ++k) {
                 const zc r = Rr[k];
-                rw = rfma(gW[(s0 + k) * n + j], r, rw);
+                rw = rfma(onishi ? gU1[(s0 + k) * n + j] : gW[(s0 + k) * n + j], r, rw);
                 b1 = rfma(gV1[(s0 + k) * n + j], r, b1);
                 b2 = rfma(gU1[(s0 + k) * n + j], zconj(r), b2);
+                cv = rfma(gV1[(s0 + k) * n + j], zconj(r), cv);
             }
             RW[t] = rw;
             Bz[t] = b1;
             Bz[nn + t] = b2;
+            if (onishi) Xz[t] = cv;
         }
         __syncthreads();
         // ---- X = (R W) R^T and the T22 partials (FP64), stored in the point arithmetic
-        for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+        for (int t = threadIdx.x; t < (onishi ? 0 : nn); t += blockDim.x) {
             const int a = t / n, c = t % n;
             const int b = p.row_blk[c], s0 = p.blk_start[b], d = p.blk_size[b];
             const zc *Rr = rot + p.blk_roff[b] + (c - s0) * d;
@@ -529,7 +533,7 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                 const Z zen = ephz[ln], zenc = zconj(zen);
                 // ---- S = Cscale [[D X D, -I], [I, -Z0]] (upper triangle)
                 const Z dpp = csz * (zep * zep), dpn = csz * (zep * zen), dnn = csz * (zen * zen);
-                for (int t = threadIdx.x; t < N * (N - 1) / 2; t += blockDim.x) {
+                for (int t = threadIdx.x; t < (onishi ? 0 : N * (N - 1) / 2); t += blockDim.x) {
                     int i, j;
                     tri_index(t, N, i, j);
                     Z v;
@@ -544,8 +548,41 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                     S[i * N + j] = v;
                 }
                 __syncthreads();
-                int under;
-                const zc pf = pfaffian_upper<Z>(S, N, vec, red, sh + 2, under);
+                int under = 0;
+                zc pf;
+                if (onishi) {
+                    // Onishi (PNAMP_Onishi.f90:21-37): sqrt(det(Ubar^T U0 + Vbar^T V0)),
+                    // Ubar = R U1, Vbar = conj(R) V1 at phi = 0; LU determinant, principal root
+                    zc *Bm = reinterpret_cast<zc *>(S);
+                    for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+                        const int i = t / n, j = t % n;
+                        zc acc2 = mk(0, 0);
+                        for (int k = 0; k < n; ++k) {
+                            acc2 = rfma(gU0[k * n + j], RW[k * n + i], acc2);
+                            acc2 = rfma(gV0[k * n + j], Xz[k * n + i], acc2);
+                        }
+                        Bm[t] = acc2;
+                    }
+                    __syncthreads();
+                    zc *invz = reinterpret_cast<zc *>(invd);
+                    const bool bsing = lu_factor<zc>(Bm, n, n, perm, invz, sh);
+                    if (threadIdx.x == 0) {
+                        zc det = mk(1.0, 0.0);
+                        for (int k = 0; k < n; ++k) {
+                            det = det * Bm[k * n + k];
+                            if (perm[k] != k) det = -det;
+                        }
+                        if (bsing) det = mk(0.0, 0.0);
+                        const double r = sqrt(det.x * det.x + det.y * det.y);
+                        const double re = sqrt(0.5 * (r + det.x)), im = copysign(sqrt(0.5 * fmax(r - det.x, 0.0)), det.y);
+                        acc[kNobs - 1] = mk(re, im);  // scratch slot: observable 19 is never set
+                    }
+                    __syncthreads();
+                    pf = acc[kNobs - 1];
+                    __syncthreads();
+                } else {
+                    pf = pfaffian_upper<Z>(S, N, vec, red, sh + 2, under);
+                }
                 // ---- T22(phi) and right-hand sides
                 for (int t = threadIdx.x; t < nn; t += blockDim.x) {
                     Z s = zep * P[t];
@@ -726,7 +763,7 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                         return fin[slot];
                     };
                     const zc zph = expi(-(twopi * lp / p.nfom * p.nprot + twopi * ln / p.nfom * p.nneut));
-                    const zc norm = (p.vacfac * det0 * det1) * (pf * zph);
+                    const zc norm = onishi ? pf : (p.vacfac * det0 * det1) * (pf * zph);
                     const zc trp = mk(get(10), get(11)), trm = mk(get(12), get(13)), trz = mk(get(14), get(15));
                     const zc j2 = mk(get(16) + get(8), get(17) + get(9)) + trp * trm + trz * trz;
                     const zc ekin = mk(get(4), get(5));
@@ -754,6 +791,7 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
         if (threadIdx.x == 0) {
             const double inv = 1.0 / ((double)p.nfom * p.nfom);
             int f = flags;
+            acc[kNobs - 1] = mk(0.0, 0.0);
             for (int io = 0; io < kNobs; ++io) {
                 const zc v = inv * acc[io];
                 if (!zfinite(v)) f |= 4;

@@ -142,3 +142,44 @@ def test_ge76_kernel_files_through_gpu(ge76, form):
                     mine = kern[name][J, JJMAX, JJMAX].real
                     ref = gold[jj, f].real
                     assert abs(mine - ref) <= 2e-7 * abs(ref) + 1e-12, ((i, j), J, name, mine, ref)
+
+
+def test_df64_form_energies_within_1kev_of_fp64():
+    """Every form must keep E_J and GCM levels within 1 keV of FP64 (the benchmark spec)."""
+    from sccm_gb300.forms import compare
+    w = make_workload("pf", 4, Mesh(4, 8, 4, 5), seed=606)
+    r = compare(w, "df64")
+    assert r["max_rel_err_norm_kernel"] <= NORM_TOL
+    assert r["max_abs_err_gcm_levels_keV"] < 1.0
+    assert r["max_abs_err_EJ_per_vacuum_keV"] < 1.0
+
+
+def test_ge76_gcm_levels_match_reference_kernel_files(ge76):
+    """Hill-Wheeler on the GPU kernels reproduces the levels from the reference's kernel files."""
+    from sccm_gb300.gcm import gcm_levels, compare_levels
+    g = ge76
+    mesh = Mesh(1, g["nbet"], 1, g["nfom"], ncosbet=g["ncosbet"])
+    pairs = [(i, j) for i in range(4) for j in range(i, 4)]
+    with PnampContext(g["sp"], g["e0"], g["t1b"], g["recs"], g["vbar"], mesh, q2=g["q2"]) as ctx:
+        z, _ = ctx.batch([(g["U"][i], g["V"][i], g["U"][j], g["V"][j]) for i, j in pairs])
+        mine = [ctx.project(z[k], chop=False) for k in range(len(pairs))]
+    ref = []
+    for (i, j) in pairs:
+        k = {f: np.zeros((7, 13, 13), complex) for f in ("njkk", "hjkk")}
+        for jj, J in enumerate(g["jvals"]):
+            k["njkk"][J, JJMAX, JJMAX] = g["gold"][i, j, jj, 0]
+            k["hjkk"][J, JJMAX, JJMAX] = g["gold"][i, j, jj, 1]
+        ref.append(k)
+    a = gcm_levels(mine, pairs, 4, jvals=(0, 2, 4), axial=True)
+    b = gcm_levels(ref, pairs, 4, jvals=(0, 2, 4), axial=True)
+    dl, dq = compare_levels(a, b, nlev=2)
+    assert dl < 1e-3 and dq < 1e-3, (dl, dq)   # MeV: within 1 keV
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_nfom1_uses_onishi_norm_like_the_reference(sd, form):
+    """NFOM = 1: Kernel3D.f90:286-290 switches to the Onishi norm (principal square root)."""
+    mesh = Mesh(2, 3, 2, 1)
+    with ctx_for(sd, mesh, form=form) as ctx:
+        r = ctx.pair(*sd.vacua[0], *sd.vacua[1])
+    assert_zres_close(r.zres, oracle_zres(sd, mesh, 0, 1))
