@@ -165,6 +165,19 @@ int pnamp_project(pnamp_ctx *ctx, const double *zres, int chop, pnamp_kernels *o
 int pnamp_project_device(pnamp_ctx *ctx, int npairs, const double *d_zres, int chop,
                          double *d_out, void *stream);
 
+/* Quadrupole reduced elements of one pair's ZRES (PNAMP_Kernel3D_v2.f90:515-600; the
+ * Kernel%qpred/qcpred blocks post_general writes, PNAMP_IO.f90:202-217):
+ * qpred[J2][dJ][K1+8][K2+6] = <J2+dJ, K1, q1 || Q2 || J2, K2, q2>, dJ = 0 (spectroscopic),
+ * 1, 2; qcpred the q1 <-> q2 exchanged element from the Q^dagger traces, computed
+ * when `exchange` is non-zero (the reference does so when q1 != q2). Each output
+ * holds (JJMAX+1)*3*17*13 complex; only even J2 are filled. Host buffers. */
+int pnamp_project_q(pnamp_ctx *ctx, const double *zres, int exchange, double *qpred, double *qcpred);
+
+/* Batched form with DEVICE buffers: d_out is [npairs][2][(JJMAX+1)*3*17*13] complex
+ * (qpred, then qcpred). */
+int pnamp_project_q_device(pnamp_ctx *ctx, int npairs, const double *d_zres, int exchange,
+                           double *d_out, void *stream);
+
 /* Synchronise the context's work; returns the first CUDA error seen. */
 int pnamp_sync(pnamp_ctx *ctx);
 

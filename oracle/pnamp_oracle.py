@@ -387,3 +387,52 @@ def project_axial(zres, mesh: Mesh, core_prot=0, core_neut=0, jmax=JJMAX):
         out["njkk"][J, o, o] = s[0]
         out["J2"][J, o, o] = s[7] / s[0]
     return out
+
+
+def project_q(zres, mesh: Mesh, exchange=True, jmax=JJMAX):
+    """Quadrupole reduced elements <J1 K1 q1||Q2||J2 K2 q2>, J1 = J2 + dJ, dJ = 0, 1, 2.
+
+    Plain D-function form of PNAMP_Kernel3D_v2.f90:515-600 (spectroscopic dJ = 0
+    and the dJ = 2 transition element; dJ = 1 is the same formula, the block
+    post_general writes at PNAMP_IO.f90:213):
+      qpred = wJ (2J1+1) sum_Omega w sum_mu (-1)^(J1-K1) (J1 2 J2; -K1 mu K2p)
+              d^J2_{K2p K2}(bet) e^{i K2p alp} e^{i K2 gam} ZRES(Omega, Q_mu),  K2p = K1 - mu
+    and, for q1 != q2, the exchanged element from the Q^dagger traces (:536-546):
+      qcpred = wJ (2J1+1) sum w sum_{mu,nu} (-1)^(J1-K1) (-1)^|mu-nu| d^2_{-nu,-mu}(bet)
+               e^{-i nu alp} e^{-i mu gam} conj(ZRES(Omega, Qt_nu)) (J1 2 J2; -K1 mu K2p)
+               d^J2_{K2 K2p}(bet) e^{-i K2 alp} e^{-i K2p gam}.
+    Returns arrays [J2][dJ][K1+8][K2+6] (only even J2 filled).
+    """
+    from sccm_gb300.basis import threej
+    pts = mesh.euler_points()
+    axial = mesh.nalp * mesh.ngam == 1
+    qp = np.zeros((jmax + 1, 3, 17, 13), complex)
+    qc = np.zeros_like(qp)
+    for J2 in range(0, jmax + 1, 2):
+        wj = (2 * J2 + 1) / 2.0 if axial else (2 * J2 + 1) / (8 * math.pi ** 2)
+        for dJ in range(3):
+            J1 = J2 + dJ
+            for K1 in range(-J1, J1 + 1):
+                for K2 in range(-J2, J2 + 1):
+                    sd = 0.0 + 0.0j
+                    sx = 0.0 + 0.0j
+                    for mu in range(-2, 3):
+                        K2p = K1 - mu
+                        if abs(K2p) > J2:
+                            continue
+                        tj = threej(2 * J1, 4, 2 * J2, -2 * K1, 2 * mu, 2 * K2p)
+                        if tj == 0.0:
+                            continue
+                        ph = (-1.0) ** (J1 - K1)
+                        for ie, (alp, bet, gam, w) in enumerate(pts):
+                            sd += (w * ph * tj * dwig(2 * J2, 2 * K2p, 2 * K2, bet)
+                                   * np.exp(1j * (K2p * alp + K2 * gam)) * zres[ie, 10 + mu])
+                            if exchange:
+                                for nu in range(-2, 3):
+                                    sx += (w * ph * (-1.0) ** abs(mu - nu) * dwig(4, -2 * nu, -2 * mu, bet)
+                                           * np.exp(-1j * (nu * alp + mu * gam)) * np.conj(zres[ie, 15 + nu])
+                                           * tj * dwig(2 * J2, 2 * K2, 2 * K2p, bet)
+                                           * np.exp(-1j * (K2 * alp + K2p * gam)))
+                    qp[J2, dJ, K1 + 8, K2 + 6] = wj * (2 * J1 + 1) * sd
+                    qc[J2, dJ, K1 + 8, K2 + 6] = wj * (2 * J1 + 1) * sx
+    return qp, qc

@@ -33,6 +33,8 @@ struct pnamp_ctx {
     long long pair_cap = 0;
     zc *d_scratch = nullptr;
     zc *d_projw = nullptr;
+    const double *d_tj = nullptr;   // 3j symbols of the Q2 projection
+    double *d_projq = nullptr;
     double *d_uv = nullptr, *d_zres = nullptr, *d_proj = nullptr;
     int *d_status = nullptr;
     long long batch_cap = 0;
@@ -62,6 +64,42 @@ int dev_upload(pnamp_ctx *c, const std::vector<T> &h, const T **out) {
     if (!h.empty()) CK(cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
     *out = d;
     return PNAMP_OK;
+}
+
+double fact_h(int k) {
+    double f = 1.0;
+    for (int i = 2; i <= k; ++i) f *= i;
+    return f;
+}
+
+// <j1 m1 j2 m2 | J M>, doubled arguments, Racah's formula
+double cg_h(int tj1, int tj2, int tJ, int tm1, int tm2, int tM) {
+    if (tm1 + tm2 != tM) return 0.0;
+    if (tJ < std::abs(tj1 - tj2) || tJ > tj1 + tj2 || (tj1 + tj2 + tJ) % 2) return 0.0;
+    if (std::abs(tm1) > tj1 || std::abs(tm2) > tj2 || std::abs(tM) > tJ) return 0.0;
+    if ((tj1 + tm1) % 2 || (tj2 + tm2) % 2 || (tJ + tM) % 2) return 0.0;
+    const double tri = fact_h((tj1 + tj2 - tJ) / 2) * fact_h((tj1 - tj2 + tJ) / 2) *
+                       fact_h((-tj1 + tj2 + tJ) / 2) / fact_h((tj1 + tj2 + tJ) / 2 + 1);
+    const double pre = std::sqrt((tJ + 1) * tri * fact_h((tj1 + tm1) / 2) * fact_h((tj1 - tm1) / 2) *
+                                 fact_h((tj2 + tm2) / 2) * fact_h((tj2 - tm2) / 2) * fact_h((tJ + tM) / 2) *
+                                 fact_h((tJ - tM) / 2));
+    double sum = 0.0;
+    for (int k = 0; k < 100; ++k) {
+        const int a1 = (tj1 + tj2 - tJ) / 2 - k, a2 = (tj1 - tm1) / 2 - k, a3 = (tj2 + tm2) / 2 - k;
+        const int a4 = (tJ - tj2 + tm1) / 2 + k, a5 = (tJ - tj1 - tm2) / 2 + k;
+        if (a1 < 0 || a2 < 0 || a3 < 0) break;
+        if (a4 < 0 || a5 < 0) continue;
+        sum += ((k & 1) ? -1.0 : 1.0) /
+               (fact_h(k) * fact_h(a1) * fact_h(a2) * fact_h(a3) * fact_h(a4) * fact_h(a5));
+    }
+    return pre * sum;
+}
+
+// Wigner 3j (j1 j2 j3; m1 m2 m3), doubled arguments
+double threej_h(int tj1, int tj2, int tj3, int tm1, int tm2, int tm3) {
+    if (tm1 + tm2 + tm3 != 0) return 0.0;
+    const double ph = (((tj1 - tj2 - tm3) / 2) % 2) ? -1.0 : 1.0;
+    return ph * cg_h(tj1, tj2, tj3, tm1, tm2, -tm3) / std::sqrt(tj3 + 1.0);
 }
 
 dd host_dd(double x) {
@@ -178,7 +216,7 @@ void pnamp_free(pnamp_ctx *ctx) {
     if (!ctx) return;
     for (void *q : ctx->allocs) cudaFree(q);
     for (void *q : {(void *)ctx->d_pairbuf, (void *)ctx->d_scratch, (void *)ctx->d_uv, (void *)ctx->d_zres,
-                    (void *)ctx->d_status, (void *)ctx->d_proj})
+                    (void *)ctx->d_status, (void *)ctx->d_proj, (void *)ctx->d_projq})
         if (q) cudaFree(q);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -382,6 +420,22 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
         pnamp_free(c);
         return PNAMP_ERR_NOMEM;
     }
+    {   // 3j symbols (J1 2 J2; -K1 mu K1-mu) in the order of project_q_kernel's outputs
+        std::vector<double> tj;
+        for (int J2 = 0; J2 <= kJJMax; J2 += 2)
+            for (int dJ = 0; dJ < 3; ++dJ) {
+                const int J1 = J2 + dJ;
+                for (int r = 0; r < (2 * J1 + 1) * (2 * J2 + 1); ++r) {
+                    const int K1 = r / (2 * J2 + 1) - J1;
+                    for (int mu = -2; mu <= 2; ++mu)
+                        tj.push_back(threej_h(2 * J1, 4, 2 * J2, -2 * K1, 2 * mu, 2 * (K1 - mu)));
+                }
+            }
+        if ((int)tj.size() != 5 * n_q_outputs() || (rc = dev_upload(c, tj, &c->d_tj)) != PNAMP_OK) {
+            pnamp_free(c);
+            return rc ? rc : PNAMP_ERR_STATE;
+        }
+    }
     if (launch_proj_weights(p, c->axial, c->d_projw, c->stream) != cudaSuccess ||
         cudaStreamSynchronize(c->stream) != cudaSuccess) {
         pnamp_free(c);
@@ -459,6 +513,33 @@ int pnamp_project(pnamp_ctx *c, const double *zres, int chop, pnamp_kernels *out
     CK(cudaStreamSynchronize(c->stream));
     double *dst[kProjFields] = {out->njkk, out->hjkk, out->nn, out->zz, out->j2};
     for (int q = 0; q < kProjFields; ++q) memcpy(dst[q], h.data() + 2 * q * fs, 2 * fs * sizeof(double));
+    return PNAMP_OK;
+}
+
+int pnamp_project_q_device(pnamp_ctx *c, int npairs, const double *d_zres, int exchange, double *d_out,
+                           void *stream) {
+    if (!c || npairs < 0 || (npairs > 0 && (!d_zres || !d_out))) return PNAMP_ERR_ARG;
+    if (npairs == 0) return PNAMP_OK;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
+    const size_t blk = (size_t)(kJJMax + 1) * 3 * 17 * 13;
+    CK(cudaMemsetAsync(d_out, 0, (size_t)npairs * 2 * 2 * blk * sizeof(double), st));
+    CK(launch_project_q(c->p, c->axial, npairs, d_zres, c->d_tj, exchange ? 1 : 0, d_out, st));
+    return PNAMP_OK;
+}
+
+int pnamp_project_q(pnamp_ctx *c, const double *zres, int exchange, double *qpred, double *qcpred) {
+    if (!c || !zres || !qpred || !qcpred) return PNAMP_ERR_ARG;
+    int rc = ensure_batch(c, 1);
+    if (rc) return rc;
+    const size_t blk = (size_t)(kJJMax + 1) * 3 * 17 * 13;
+    if (!c->d_projq) CK(cudaMalloc(&c->d_projq, 2 * 2 * blk * sizeof(double)));
+    const size_t zbytes = (size_t)2 * kNobs * c->p.n_euler * sizeof(double);
+    CK(cudaMemcpyAsync(c->d_zres, zres, zbytes, cudaMemcpyHostToDevice, c->stream));
+    rc = pnamp_project_q_device(c, 1, c->d_zres, exchange, c->d_projq, c->stream);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(qpred, c->d_projq, 2 * blk * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(qcpred, c->d_projq + 2 * blk, 2 * blk * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
     return PNAMP_OK;
 }
 

@@ -88,6 +88,9 @@ cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc
 cudaError_t launch_proj_weights(const Params &p, int axial, zc *w, cudaStream_t st);
 cudaError_t launch_project(const Params &p, int npairs, const zc *w, const double *zres,
                            int core_prot, int core_neut, int chop, double *out, cudaStream_t st);
+cudaError_t launch_project_q(const Params &p, int axial, int npairs, const double *zres, const double *tj,
+                             int exchange, double *out, cudaStream_t st);
+int n_q_outputs();
 cudaError_t set_point_smem(int form, int bytes);
 cudaError_t point_blocks_per_sm(int form, int smem_bytes, int *per_sm);
 int setup_smem_bytes(int n);

@@ -895,6 +895,82 @@ cudaError_t launch_project(const Params &p, int npairs, const zc *w, const doubl
     return cudaGetLastError();
 }
 
+// Quadrupole reduced elements <J1 K1||Q2||J2 K2>, J1 = J2 + dJ, dJ = 0, 1, 2
+// (PNAMP_Kernel3D_v2.f90:515-600): one thread per (J2, dJ, K1, K2) output,
+// direct and, when `exchange`, the q1 <-> q2 exchanged element from the Q^dagger
+// traces. `tj` holds the 3j symbols (J1 2 J2; -K1 mu K2p) per output and mu.
+// Output [pair][2][7][3][17][13] complex (direct, exchanged), zeroed beforehand.
+__global__ void project_q_kernel(Params p, int axial, const double *__restrict__ zres, const double *__restrict__ tj,
+                                 int exchange, double *__restrict__ out) {
+    const int pair = blockIdx.x;
+    const int o = blockIdx.y * blockDim.x + threadIdx.x;  // index into the (J2, dJ, K1, K2) list
+    int J2 = 0, dJ = 0, rem = o, found = 0;
+    for (J2 = 0; J2 <= kJJMax && !found; J2 += 2)
+        for (dJ = 0; dJ < 3; ++dJ) {
+            const int cnt = (2 * (J2 + dJ) + 1) * (2 * J2 + 1);
+            if (rem < cnt) {
+                found = 1;
+                break;
+            }
+            rem -= cnt;
+        }
+    if (!found) return;
+    J2 -= 2;  // undo the outer loop's final increment
+    const int J1 = J2 + dJ;
+    const int K1 = rem / (2 * J2 + 1) - J1, K2 = rem % (2 * J2 + 1) - J2;
+    const double *z = zres + 2LL * pair * kNobs * p.n_euler;
+    zc sd = mk(0, 0), sx = mk(0, 0);
+    for (int ie = 0; ie < p.n_euler; ++ie) {
+        const double alp = p.euler[4 * ie], bet = p.euler[4 * ie + 1], gam = p.euler[4 * ie + 2],
+                     w = p.euler[4 * ie + 3];
+        double cb, sb;
+        sincos(0.5 * bet, &sb, &cb);
+        for (int mu = -2; mu <= 2; ++mu) {
+            const int K2p = K1 - mu;
+            const double t3 = tj[5 * o + mu + 2];
+            if (K2p > J2 || -K2p > J2 || t3 == 0.0) continue;
+            const double ph = ((J1 - K1) & 1) ? -1.0 : 1.0;
+            const zc zq = mk(z[2LL * ((10 + mu) * p.n_euler + ie)], z[2LL * ((10 + mu) * p.n_euler + ie) + 1]);
+            const double d1 = wigner_d(2 * J2, 2 * K2p, 2 * K2, cb, sb, p.fact);
+            sd = zfma((w * ph * t3 * d1) * expi(K2p * alp + K2 * gam), zq, sd);
+            if (exchange) {
+                const double d2 = wigner_d(2 * J2, 2 * K2, 2 * K2p, cb, sb, p.fact);
+                const zc e2 = expi(-(K2 * alp + K2p * gam));
+                for (int nu = -2; nu <= 2; ++nu) {
+                    const int ix = 15 + nu;
+                    const zc zt = mk(z[2LL * (ix * p.n_euler + ie)], -z[2LL * (ix * p.n_euler + ie) + 1]);
+                    const double sg = ((mu - nu) & 1) ? -1.0 : 1.0;
+                    const double dq = wigner_d(4, -2 * nu, -2 * mu, cb, sb, p.fact);
+                    sx = zfma((w * ph * sg * dq * t3 * d2) * (expi(-(nu * alp + mu * gam)) * e2), zt, sx);
+                }
+            }
+        }
+    }
+    const double wj = axial ? (2.0 * J2 + 1.0) / 2.0 : (2.0 * J2 + 1.0) / (8.0 * M_PI * M_PI);
+    const double f = wj * (2 * J1 + 1);
+    const long long blk = 7LL * 3 * 17 * 13;
+    const long long idx = (((long long)J2 * 3 + dJ) * 17 + (K1 + 8)) * 13 + (K2 + 6);
+    double *op = out + 2LL * pair * 2 * blk;
+    op[2 * idx] = f * sd.x;
+    op[2 * idx + 1] = f * sd.y;
+    op[2 * (blk + idx)] = f * sx.x;
+    op[2 * (blk + idx) + 1] = f * sx.y;
+}
+
+int n_q_outputs() {
+    int c = 0;
+    for (int J2 = 0; J2 <= kJJMax; J2 += 2)
+        for (int dJ = 0; dJ < 3; ++dJ) c += (2 * (J2 + dJ) + 1) * (2 * J2 + 1);
+    return c;
+}
+
+cudaError_t launch_project_q(const Params &p, int axial, int npairs, const double *zres, const double *tj,
+                             int exchange, double *out, cudaStream_t st) {
+    dim3 grid(npairs, (n_q_outputs() + 127) / 128);
+    project_q_kernel<<<grid, 128, 0, st>>>(p, axial, zres, tj, exchange, out);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_proj_weights(const Params &p, int axial, zc *w, cudaStream_t st) {
     proj_weights_kernel<<<p.n_euler, 128, 0, st>>>(p, axial, w);
     return cudaGetLastError();

@@ -15,9 +15,7 @@ from __future__ import annotations
 import json
 import os
 
-import numpy as np
-
-from .formats import atomic_write_text, write_elem_general
+from .formats import atomic_write_text, empty_kernels, write_elem_general
 from .pnamp import PnampContext
 
 
@@ -57,9 +55,10 @@ def run_pairs(ctx: PnampContext, vacua, pairs, out_dir, prefix="kern", coords=No
             kern = ctx.project(zres[k], chop=True)
             c1 = coords[q1 - 1] if coords is not None else (0.0, 0.0)
             c2 = coords[q2 - 1] if coords is not None else (0.0, 0.0)
-            zero = np.zeros((7, 13, 13, 3), complex)
-            full = dict(kern, q0p=np.zeros((7, 13, 13), complex), q0pc=np.zeros((7, 13, 13), complex),
-                        qpred=zero, qcpred=zero)
+            full = empty_kernels()
+            full.update(kern)
+            # the reference computes the exchanged element only for q1 != q2 (Kernel3D.f90:620,674)
+            full["qpred"], full["qcpred"] = ctx.project_q(zres[k], exchange=(q1 != q2))
             atomic_write_text(os.path.join(out_dir, elem_name(prefix, q1, q2)), write_elem_general,
                               full, c1, c2)
             done.add((q1, q2))

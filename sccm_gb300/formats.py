@@ -71,7 +71,7 @@ def read_wf(path, nlev):
         if len(head) < 2:
             raise FormatError(f"{path}: missing ide header")
         ide = (int(head[0]), int(head[1]))
-        data = np.array(f.read().split(), dtype=np.float64) if True else None
+        data = np.array(f.read().split(), dtype=np.float64)
     want = 2 * nlev * nlev
     if data.size < want:
         raise FormatError(f"{path}: truncated ({data.size} of {want} values)")
@@ -230,6 +230,15 @@ def _line(vals):
     return "".join(out)
 
 
+def empty_kernels():
+    """Zeroed kernel-file fields: [J][K1+6][K2+6] scalars, [J][dJ][K1+8][K2+6] quadrupole blocks."""
+    sh = (JJMAX + 1, 2 * JJMAX + 1, 2 * JJMAX + 1)
+    out = {k: np.zeros(sh, complex) for k in ("njkk", "hjkk", "nn", "zz", "J2", "q0p", "q0pc")}
+    out["qpred"] = np.zeros((JJMAX + 1, 3, 17, 13), complex)
+    out["qcpred"] = np.zeros_like(out["qpred"])
+    return out
+
+
 def write_elem_axial(path, kern, q1=(0.0, 0.0), q2=(0.0, 0.0), jmin=0, jmax=JJMAX, jstep=2):
     """`post_axial` layout (PNAMP_IO.f90:2-36); `kern` maps field -> array [J][K1][K2]."""
     with open(path, "w") as f:
@@ -244,8 +253,8 @@ def write_elem_axial(path, kern, q1=(0.0, 0.0), q2=(0.0, 0.0), jmin=0, jmax=JJMA
             f.write(_line([g("nn"), g("zz")]) + "\n")
             f.write(_line([g("J2")]) + "\n")
             f.write(_line([g("q0p"), g("q0pc")]) + "\n")
-            for mu in range(3):
-                f.write(_line([kern["qpred"][J, JJMAX, JJMAX, mu], kern["qcpred"][J, JJMAX, JJMAX, mu]]) + "\n")
+            for dj in range(3):
+                f.write(_line([kern["qpred"][J, dj, 8, 6], kern["qcpred"][J, dj, 8, 6]]) + "\n")
 
 
 def write_elem_general(path, kern, q1=(0.0, 0.0), q2=(0.0, 0.0), jmin=0, jmax=JJMAX, jstep=1):
@@ -264,16 +273,58 @@ def write_elem_general(path, kern, q1=(0.0, 0.0), q2=(0.0, 0.0), jmin=0, jmax=JJ
                     f.write(_line([g("njkk"), g("hjkk")]) + "\n")
                     f.write(_line([g("nn"), g("zz")]) + "\n")
                     f.write(_line([g("J2")]) + "\n")
-                    f.write(_line([kern["qpred"][J, k1 + JJMAX, k2 + JJMAX, 0],
-                                   kern["qcpred"][J, k1 + JJMAX, k2 + JJMAX, 0]]) + "\n")
+                    f.write(_line([kern["qpred"][J, 0, k1 + 8, k2 + 6],
+                                   kern["qcpred"][J, 0, k1 + 8, k2 + 6]]) + "\n")
                     f.write(_line([g("q0p"), g("q0pc")]) + "\n")
             for k2 in range(-k2max, k2max + 1):
                 for k1 in range(-k2max - 1, k2max + 2):
-                    f.write(_line([kern["qpred"][J, k1 + JJMAX, k2 + JJMAX, 1],
-                                   kern["qcpred"][J, k1 + JJMAX, k2 + JJMAX, 1]]) + "\n")
+                    f.write(_line([kern["qpred"][J, 1, k1 + 8, k2 + 6],
+                                   kern["qcpred"][J, 1, k1 + 8, k2 + 6]]) + "\n")
                 for k1 in range(-k2max - 2, k2max + 3):
-                    f.write(_line([kern["qpred"][J, k1 + JJMAX, k2 + JJMAX, 2],
-                                   kern["qcpred"][J, k1 + JJMAX, k2 + JJMAX, 2]]) + "\n")
+                    f.write(_line([kern["qpred"][J, 2, k1 + 8, k2 + 6],
+                                   kern["qcpred"][J, 2, k1 + 8, k2 + 6]]) + "\n")
+
+
+def read_elem_general(path, jmin=0, jmax=JJMAX, jstep=1):
+    """Parse a `post_general` file (the layout write_elem_general produces) into kernel fields."""
+    with open(path) as f:
+        lines = [ln.rstrip("\n") for ln in f if ln.strip()]
+
+    def nums(s):
+        return [float(s[k:k + 15]) for k in range(0, len(s) - 14, 15)]
+    out = empty_kernels()
+    coords = {}
+    i = 0
+    for J in range(jmin, jmax + 1, jstep):
+        if J == 1:
+            continue
+        if int(lines[i].split()[0]) != J:
+            raise FormatError(f"{path}: expected J = {J}")
+        coords[J] = nums(lines[i + 1])
+        i += 2
+        k2max = J if J % 2 == 0 else abs(J - 1)
+        for k2 in range(-k2max, k2max + 1):
+            for k1 in range(-k2max, k2max + 1):
+                kk = [int(x) for x in lines[i].split()]
+                if kk != [k1, k2]:
+                    raise FormatError(f"{path}: expected K1 K2 = {k1} {k2}")
+                r = [nums(lines[i + 1 + q]) for q in range(5)]
+                c = lambda v, q: complex(v[2 * q], v[2 * q + 1])
+                ix = (J, k1 + JJMAX, k2 + JJMAX)
+                out["njkk"][ix], out["hjkk"][ix] = c(r[0], 0), c(r[0], 1)
+                out["nn"][ix], out["zz"][ix] = c(r[1], 0), c(r[1], 1)
+                out["J2"][ix] = c(r[2], 0)
+                out["qpred"][J, 0, k1 + 8, k2 + 6], out["qcpred"][J, 0, k1 + 8, k2 + 6] = c(r[3], 0), c(r[3], 1)
+                out["q0p"][ix], out["q0pc"][ix] = c(r[4], 0), c(r[4], 1)
+                i += 6
+        for k2 in range(-k2max, k2max + 1):
+            for dj, span in ((1, k2max + 1), (2, k2max + 2)):
+                for k1 in range(-span, span + 1):
+                    v = nums(lines[i])
+                    out["qpred"][J, dj, k1 + 8, k2 + 6] = complex(v[0], v[1])
+                    out["qcpred"][J, dj, k1 + 8, k2 + 6] = complex(v[2], v[3])
+                    i += 1
+    return out, coords
 
 
 def read_elem_axial(path):

@@ -42,7 +42,8 @@ _lib = None
 # Every symbol the public header declares (tests check the library exports them).
 EXPORTS = ("pnamp_init", "pnamp_n_euler", "pnamp_pair", "pnamp_batch", "pnamp_batch_device",
            "pnamp_project", "pnamp_project_device", "pnamp_sync", "pnamp_free",
-           "pnamp_strerror", "pnamp_version", "pnamp_batch_device_noalloc", "pnamp_set_form")
+           "pnamp_strerror", "pnamp_version", "pnamp_batch_device_noalloc", "pnamp_set_form",
+           "pnamp_project_q", "pnamp_project_q_device")
 FORMS = {"fp64": 0, "df64": 1}
 PNAMP_ERR_SCRATCH_LIMIT = 7
 
@@ -101,6 +102,9 @@ def load_library(path: str | None = None):
     lib.pnamp_batch_device_noalloc.argtypes = [vp, C.c_int, vp, vp, vp, vp]
     lib.pnamp_project.argtypes = [vp, C.POINTER(C.c_double), C.c_int, C.POINTER(_Kernels)]
     lib.pnamp_project_device.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp]
+    lib.pnamp_project_q.argtypes = [vp, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double),
+                                    C.POINTER(C.c_double)]
+    lib.pnamp_project_q_device.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp]
     lib.pnamp_sync.argtypes = [vp]
     lib.pnamp_free.argtypes = [vp]
     lib.pnamp_free.restype = None
@@ -250,6 +254,20 @@ class PnampContext:
         if rc != PNAMP_OK:
             raise PnampError(rc, "pnamp_project")
         return out
+
+    def project_q(self, zres, exchange=True):
+        """Quadrupole reduced elements -> (qpred, qcpred), each [J2, dJ, K1+8, K2+6] complex."""
+        z = np.ascontiguousarray(np.asarray(zres, dtype=np.complex128).T)
+        if z.shape != (NOBS, self.n_euler):
+            raise ValueError("zres must be [P_E, NOBS]")
+        qp = np.zeros((JJMAX + 1, 3, 17, 13), dtype=np.complex128)
+        qc = np.zeros_like(qp)
+        rc = load_library().pnamp_project_q(self._h, z.ctypes.data_as(C.POINTER(C.c_double)),
+                                            1 if exchange else 0, qp.ctypes.data_as(C.POINTER(C.c_double)),
+                                            qc.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_project_q")
+        return qp, qc
 
     # device-pointer entry points (inputs already resident in HBM)
     def batch_device(self, npairs, d_uv, d_zres, d_status, stream=0):

@@ -6,6 +6,8 @@ Tolerances (FP64 throughout):
   * projected fields vs the reference's Ge76 kernel files: 2e-7 relative
     (the files print 8 significant digits)
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -183,3 +185,36 @@ def test_nfom1_uses_onishi_norm_like_the_reference(sd, form):
     with ctx_for(sd, mesh, form=form) as ctx:
         r = ctx.pair(*sd.vacua[0], *sd.vacua[1])
     assert_zres_close(r.zres, oracle_zres(sd, mesh, 0, 1))
+
+
+def test_quadrupole_projection_matches_oracle(sd):
+    """<J1 K1||Q2||J2 K2>, dJ = 0, 1, 2, direct and exchanged (PNAMP_Kernel3D_v2.f90:515-600)."""
+    from oracle.pnamp_oracle import project_q
+    mesh = Mesh(2, 3, 2, 2)
+    z = oracle_zres(sd, mesh, 0, 1)
+    qp_ref, qc_ref = project_q(z, mesh, exchange=True, jmax=4)
+    with ctx_for(sd, mesh) as ctx:
+        qp, qc = ctx.project_q(z, exchange=True)
+    for got, ref in ((qp, qp_ref), (qc, qc_ref)):
+        scale = np.abs(ref).max()
+        assert scale > 0
+        assert np.abs(got[:5] - ref[:5]).max() <= 1e-12 * scale
+
+
+def test_driver_writes_kernel_files_and_resumes(sd, tmp_path):
+    """PNAMP_Main's loop for one rank: kernel files written atomically, manifest resumes."""
+    from sccm_gb300.driver import pair_list, rank_pairs, run_pairs, elem_name
+    from sccm_gb300.formats import read_elem_general
+    pairs = pair_list(1, 2, 1, 2, icons=0)
+    with ctx_for(sd, sd.mesh) as ctx:
+        done = run_pairs(ctx, sd.vacua, rank_pairs(pairs, 0, 1), str(tmp_path), batch=2)
+        assert done == pairs
+        z, _ = ctx.batch([(*sd.vacua[0], *sd.vacua[1])])
+        kern = ctx.project(z[0])
+        before = os.path.getmtime(tmp_path / elem_name("kern", 1, 2))
+        run_pairs(ctx, sd.vacua, pairs, str(tmp_path))          # nothing left to do
+        assert os.path.getmtime(tmp_path / elem_name("kern", 1, 2)) == before
+    r, _ = read_elem_general(tmp_path / elem_name("kern", 1, 2))
+    for f in ("njkk", "hjkk"):
+        sc = np.abs(kern[f]).max()
+        assert np.abs(r[f][::2] - kern[f][::2]).max() <= 1e-7 * sc
