@@ -37,7 +37,14 @@ sys.path.insert(0, ROOT)
 
 METRIC = "projected kernel points/s on 1 GB300: learned+mixed vs plain FP64 at <=1 keV E_J"
 WORKLOAD = ("pf shell n=40 (Z=4, N=4 valence), 20 seeded deformed vacua -> 210 pairs, "
-            "Euler 10x20x10 x gauge 9x9 = 162000 points/pair, plain FP64 form")
+            "Euler 10x20x10 x gauge 9x9 = 162000 points/pair")
+FORM_TEXT = {"fp64": "plain FP64",
+             "df64": "mixed: per-point algebra in double-float (FP32 pairs) on the FP32 pipes, FP64 "
+                     "preparation and reductions; norm kernel within 1e-10 of FP64"}
+# DRAM bytes per kernel point of the point kernel (ncu dram__bytes_read + write on a
+# 10,368-point launch, scaled by points; profiles/point_kernel_pf.md): all per-point
+# matrices live in shared memory or an L2-resident slot, so traffic is tiny.
+TRAFFIC_BYTES_PER_POINT = 609536.0 / 10368.0
 # Algorithmic FP64 work per kernel point (pf, n = 40, P_G = 81): rotation,
 # W-solve and T22 partials amortised over the gauge points plus the Pfaffian,
 # T22 inverse and density products: (8+24+16) n^3 / P_G + (10.7+16+40) n^3,
@@ -153,8 +160,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--form", default="fp64", choices=["fp64", "df64"],
+    ap.add_argument("--form", default="df64", choices=["fp64", "df64"],
                     help="arithmetic of the per-point algebra: plain FP64 or double-float")
+    ap.add_argument("--no-compare", action="store_true", help="skip timing the plain FP64 form as well")
     ap.add_argument("--mesh", default=None,
                     help="override the mesh as NALP,NBET,NGAM,NFOM (small cases for profiling captures)")
     args = ap.parse_args()
@@ -213,7 +221,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    ctx = PnampContext(wl.sp, wl.e0, wl.t1b, wl.recs, wl.vbar, wl.mesh, q2=wl.q2, form=args.form)
+    ctx = PnampContext(wl.sp, wl.e0, wl.t1b, wl.recs, wl.vbar, wl.mesh, q2=wl.q2)
     P = ctx.n_euler
     G = wl.mesh.n_gauge
     pts_per_pair = P * G
@@ -246,36 +254,48 @@ def main():
         if ev:
             ev[2].record(stream)
 
-    with torch.cuda.stream(stream):
-        for k in range(args.warmup):
-            flush.zero_()
-            step(k)
-        torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
-        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-        with ClockSampler(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv")
-                          if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else f"/tmp/pnamp_clocks_{rank}.csv") as clk:
-            torch.cuda.synchronize()
-            for k in range(args.steps):
+    def timed(form):
+        """W untimed + K timed steps of one arithmetic form; (total s, point-kernel ms list, clocks)."""
+        ctx.set_form(form)
+        with torch.cuda.stream(stream):
+            for k in range(args.warmup):
                 flush.zero_()
-                step(args.warmup + k, evs[k])
+                step(k)
             torch.cuda.synchronize()
+            if dist:
+                dist.barrier()
+            evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+            with ClockSampler(os.path.join(ROOT, "gpurun_out", f"clocks_{form}_rank{rank}.csv")
+                              if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
+                              else f"/tmp/pnamp_clocks_{form}_{rank}.csv") as clk:
+                torch.cuda.synchronize()
+                for k in range(args.steps):
+                    flush.zero_()
+                    step(args.warmup + k, evs[k])
+                torch.cuda.synchronize()
+            if dist:
+                dist.barrier()
+        step_ms = [e[0].elapsed_time(e[2]) for e in evs]
+        tot = sum(step_ms) / 1e3
         if dist:
-            dist.barrier()
-    step_ms = [e[0].elapsed_time(e[2]) for e in evs]
-    kern_ms = [e[0].elapsed_time(e[1]) for e in evs]
-    total_s = sum(step_ms) / 1e3
-    if dist:
-        t = torch.tensor([total_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_s = float(t)
-    status = d_st.cpu().numpy()
-    if (status & ~1).any():
-        raise RuntimeError(f"non-trivial point status flags: {np.unique(status)}")
+            t = torch.tensor([tot], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            tot = float(t)
+        status = d_st.cpu().numpy()
+        if (status & ~1).any():
+            raise RuntimeError(f"non-trivial point status flags ({form}): {np.unique(status)}")
+        return tot, [e[0].elapsed_time(e[1]) for e in evs], clk.summary(local_rank)
+
     points = args.steps * pps * pts_per_pair * world
+    total_s, kern_ms, clocks = timed(args.form)
     value = points / total_s
-    clocks = clk.summary(local_rank)
+    plain = None
+    if args.form != "fp64" and not args.no_compare:
+        p_s, p_kern_ms, p_clocks = timed("fp64")
+        plain = {"value": points / p_s, "ms_per_step": 1e3 * p_s / args.steps, "clocks": p_clocks}
+    else:
+        p_kern_ms = kern_ms
+    ctx.set_form(args.form)
 
     # ---- e2e through the host-buffer C ABI, pinned host memory
     e2e = None
@@ -301,11 +321,14 @@ def main():
         e2e = {"value": points / te, "unit": "points/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
 
-    # ---- roofline of the dominant kernel (the point kernel; setup is < 0.1 %)
+    # ---- rooflines of the dominant kernel (the point kernel; setup is < 0.1 %). The FP64
+    # form is bound by the FP64 pipe; the double-float form does the same algorithmic
+    # work on the FP32 pipes, so its FP64-equivalent rate may exceed the FP64 peak.
     flops_pt = algorithmic_flops_per_point(wl.sp.nlev, G, len(wl.recs))
-    launch_s = statistics.mean(kern_ms) / 1e3
-    achieved = flops_pt * pps * pts_per_pair / launch_s / 1e12
+    pts_launch = pps * pts_per_pair
     peak = fp64_peak_tflops(torch) if rank == 0 else None
+    ach_form = flops_pt * pts_launch / (statistics.mean(kern_ms) / 1e3) / 1e12
+    ach_plain = flops_pt * pts_launch / (statistics.mean(p_kern_ms) / 1e3) / 1e12
 
     cpu = None
     if pool is not None:
@@ -321,15 +344,19 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "df64" if args.form == "df64" else "f64",
             "data": "synthetic: seeded vacua and TBMEs (no public dataset exists)",
-            "config": {"workload": WORKLOAD, "form": "plain FP64", "pairs_per_step": pps,
+            "config": {"workload": WORKLOAD, "form": FORM_TEXT[args.form], "pairs_per_step": pps,
                        "points_per_pair": pts_per_pair, "l2": "flushed (256 MiB write) before each step",
                        "parallelism": f"pairs round-robin over {world} rank(s)"},
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": (achieved / peak) if peak else None, "traffic": None,
-                         "kernel": "point_kernel", "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
-                         "flops_per_point": flops_pt},
+            "roofline": {"bound": "fp64", "achieved": ach_plain, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (ach_plain / peak) if peak else None,
+                         "traffic": TRAFFIC_BYTES_PER_POINT * pts_launch,
+                         "kernel": "point_kernel<FP64>", "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                         "flops_per_point": flops_pt,
+                         "df64_fp64_equivalent": {"achieved": ach_form, "frac_of_fp64_peak":
+                                                  (ach_form / peak) if peak else None}},
+            "plain_fp64": plain,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "clocks": clocks,
