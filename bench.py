@@ -150,6 +150,67 @@ def fp64_peak_tflops(torch):
     return 2 * 4096 ** 3 / best / 1e12
 
 
+UNEVEN_WORKLOAD = ("uneven batch: 64 sd pairs (n=24, Euler 8x16x8, gauge 7x7), 128 pf pairs (n=40, "
+                   "10x20x10, 9x9), 16 sd+pf pairs (n=64, 12x24x12, 11x11)")
+
+
+def uneven_main(args):
+    """`--workload uneven`: the three-model-space batch in persistent launches.
+
+    One step = one replay of the captured CUDA graph (per-context setup
+    kernels, counter resets, the persistent point kernel of each group of
+    contexts) over the whole batch, with the groups, shared-memory budgets and
+    schedule the autotuner picked (timed on the batch divided by
+    `--tune-scale`). Beside it: the same work as one `pnamp_batch_device`
+    launch per model space on one stream.
+    """
+    import torch
+    from sccm_gb300.synth import uneven_workloads
+    from sccm_gb300.uneven import UnevenBatch, autotune, time_launches
+
+    torch.cuda.set_device(0)
+    wls = uneven_workloads(args.uneven_scale)
+    ub = UnevenBatch(wls, form=args.form)
+    probe = UnevenBatch(uneven_workloads(args.uneven_scale * args.tune_scale), form=args.form)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    tune = autotune(ub, probe=probe, cache=not args.no_tune_cache)
+    probe.close()
+    ub.capture()
+    for _ in range(max(0, args.warmup - 1)):
+        ub.replay()
+    torch.cuda.synchronize()
+    with ClockSampler(os.path.join(ROOT, "gpurun_out", "clocks_uneven.csv")
+                      if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/pnamp_clocks_uneven.csv") as clk:
+        g_ms, g_all = time_launches(ub.replay, args.steps, flush=flush.zero_)
+    st = [s.cpu().numpy() for s in ub.status]
+    if any((x & ~1).any() for x in st):
+        raise RuntimeError("non-trivial point status flags in the uneven batch")
+
+    def per_context():
+        s = torch.cuda.current_stream().cuda_stream
+        for c, np_, uv, z, stt in zip(ub.ctxs, ub.npairs, ub.uv, ub.zres, ub.status):
+            c.batch_device(np_, uv.data_ptr(), z.data_ptr(), stt.data_ptr(), s)
+    per_context()
+    s_ms, _ = time_launches(per_context, max(1, min(args.steps, 2)), flush=flush.zero_)
+    print(json.dumps({
+        "metric": "projected kernel points/s, uneven batch in persistent launches (one CUDA graph)", "value": ub.points / (g_ms / 1e3),
+        "unit": "points/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": g_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "df64" if args.form == "df64" else "f64", "data": "synthetic: seeded vacua and TBMEs",
+        "config": {"workload": UNEVEN_WORKLOAD if args.uneven_scale == 1 else
+                   UNEVEN_WORKLOAD + f", pair counts / {args.uneven_scale}",
+                   "points": ub.points, "items": ub.nitems, "form": FORM_TEXT[args.form],
+                   "l2": "flushed (256 MiB write) before each step"},
+        "step_ms": g_all, "tuning": {"schedule": tune["schedule"], "groups": tune["groups"],
+                                     "smem_budgets": tune["budgets"],
+                                     "smem_bytes": [p.smem_bytes for p in ub.plans], "cached": tune["cached"],
+                                     "probe_ms": tune.get("ms")},
+        "per_context_launches": {"value": ub.points / (s_ms / 1e3), "ms_per_step": s_ms},
+        "clocks": clk.summary(0), "gpu_launches": len(ub.ctxs) + len(ub.plans)}))
+    ub.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -165,7 +226,15 @@ def main():
     ap.add_argument("--no-compare", action="store_true", help="skip timing the plain FP64 form as well")
     ap.add_argument("--mesh", default=None,
                     help="override the mesh as NALP,NBET,NGAM,NFOM (small cases for profiling captures)")
+    ap.add_argument("--workload", default="pf", choices=["pf", "uneven"],
+                    help="pf: the 210-pair pf-shell set (headline); uneven: three model spaces in one launch")
+    ap.add_argument("--uneven-scale", type=int, default=1, help="divide the uneven batch's pair counts")
+    ap.add_argument("--tune-scale", type=int, default=16,
+                    help="the autotuner times schedules on the uneven batch divided by this")
+    ap.add_argument("--no-tune-cache", action="store_true")
     args = ap.parse_args()
+    if args.workload == "uneven":
+        return uneven_main(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

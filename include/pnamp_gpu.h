@@ -126,8 +126,8 @@ int pnamp_pair(pnamp_ctx *ctx, const double *U0, const double *V0,
 
 /* A batch of pairs, host buffers. uv is [npairs][4][n*n]: U0, V0, U1, V1 of
  * each pair, column-major; zres is [npairs][NOBS*P_E]; point_status is
- * [npairs][P_E] or NULL. This is the cfg3-style batched entry the per-pair
- * MPI round robin of PNAMP_Main.f90:79-84 feeds. */
+ * [npairs][P_E] or NULL. The per-pair MPI round robin of PNAMP_Main.f90:79-84
+ * feeds this batched entry. */
 int pnamp_batch(pnamp_ctx *ctx, int npairs, const double *uv, double *zres, int *point_status);
 
 /* Same as pnamp_batch with DEVICE buffers, enqueued on `stream` (a
@@ -183,6 +183,51 @@ int pnamp_sync(pnamp_ctx *ctx);
 
 /* Free the context and its device memory. */
 void pnamp_free(pnamp_ctx *ctx);
+
+/* ---- Uneven batches: several contexts in one persistent launch ----------
+ * No reference counterpart: the reference runs one (q, q') pair at a time per
+ * MPI rank (Codes/PNAMP/PNAMP_Main.f90:79-115), each pair looping over its own
+ * Euler mesh. Here pairs of different model spaces and meshes (all contexts
+ * in the same form) are cut into (context, pair, Euler point) items that the
+ * CTAs of ONE persistent launch take from a device counter in the order of a
+ * schedule. Results land in each context's own d_zres / d_status exactly as
+ * pnamp_batch_device would write them.
+ *
+ * pnamp_multi_create allocates everything (pair records, per-CTA scratch,
+ * work list) and copies each context's parameters: the contexts and the
+ * device buffers d_uv[c] ([npairs[c]][4][n][n] column-major), d_zres[c] and
+ * d_status[c] stay owned by the caller and must outlive the plan, and a later
+ * pnamp_set_form on a context does not change a plan made before it. pnamp_multi_launch enqueues only kernels and a memset on `stream`
+ * (NULL: legacy default stream), so it may be captured into a CUDA graph and
+ * replayed; a plan must not be launched on two streams at once. */
+typedef struct pnamp_multi pnamp_multi;
+
+/* nctx = 1..4 (PNAMP_ERR_UNSUPPORTED above: every context's parameters travel
+ * by value in the launch). */
+int pnamp_multi_create(int nctx, pnamp_ctx *const *ctxs, const int *npairs,
+                       const double *const *d_uv, double *const *d_zres,
+                       int *const *d_status, pnamp_multi **out);
+
+/* Work order: order 0 = contexts as given, 1 = heaviest per-item cost first
+ * (gauge points x n^3), 2 = round robin over contexts item by item; grab =
+ * items a CTA takes per counter increment (1..64); grid = CTAs (0: one per
+ * resident slot on the device). The default after create is (1, 1, 0). */
+int pnamp_multi_schedule(pnamp_multi *plan, int order, int grab, int grid);
+
+/* Shared-memory budget per CTA (bytes; 0 = the device maximum, the default):
+ * each context's per-point arrays are re-placed (shared memory vs the CTA's
+ * global slot) under the budget and the launch holds the largest result,
+ * written to *smem_bytes when that is not NULL. What a CTA does not take as
+ * shared memory serves as L1, so a smaller budget can be faster when one
+ * context's arrays do not fit anyway. Not while a launch of the plan runs. */
+int pnamp_multi_placement(pnamp_multi *plan, int smem_budget, int *smem_bytes);
+
+int pnamp_multi_launch(pnamp_multi *plan, void *stream);
+
+/* Number of (context, pair, Euler point) items; -1 for a NULL plan. */
+int pnamp_multi_items(const pnamp_multi *plan);
+
+void pnamp_multi_free(pnamp_multi *plan);
 
 /* Static text for a return code. */
 const char *pnamp_strerror(int code);

@@ -130,9 +130,13 @@ int plan_placement(Params &p, int smem_max) {
     // the Pfaffian matrix (N^2) shares storage with rho, kappa10, kappa01, K (4 n (n+1))
     const long long s_elems = std::max<long long>((long long)N * N, 4LL * n * (n + 1));
     const int bs = (int)(s_elems * 16), bt = (int)(nn * 16), by = (int)(2 * nn * 16), buv = (int)(2 * nn * 8);
-    // greedy: keep the hottest arrays in shared memory
+    // Greedy: spill UV first, then Y, T and last S (the Pfaffian matrix, the most
+    // reused). Measured at n = 64, where S alone exceeds 227 KB: everything in the
+    // global slot with the freed shared memory serving as L1 beats keeping T + Y
+    // in shared memory, so the greedy order (which ends with all four spilled)
+    // is kept rather than a fullest-fit choice.
     int flags[4] = {1, 1, 1, 1};  // s, t, y, uv
-    const int order[4] = {3, 2, 1, 0};  // spill uv first, then y, t, s
+    const int order[4] = {3, 2, 1, 0};
     auto total = [&]() { return fixed + flags[0] * bs + flags[1] * bt + flags[2] * by + flags[3] * buv; };
     for (int k = 0; k < 4 && total() > smem_max; ++k) flags[order[k]] = 0;
     if (total() > smem_max) return PNAMP_ERR_UNSUPPORTED;
@@ -393,7 +397,12 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
         pnamp_free(c);
         return PNAMP_ERR_CUDA;
     }
-    if ((rc = plan_placement(p, smem_optin)) != PNAMP_OK) {
+    if (prepare_setup(n) != cudaSuccess) {
+        pnamp_free(c);
+        return PNAMP_ERR_CUDA;
+    }
+    // kMultiSmemTail bytes stay free at the end for the multi-context kernel's work counter
+    if ((rc = plan_placement(p, smem_optin - kMultiSmemTail)) != PNAMP_OK) {
         pnamp_free(c);
         return rc;
     }
@@ -604,3 +613,185 @@ extern "C" int pnamp_batch_device_noalloc(pnamp_ctx *c, int npairs, const double
     CK(launch_points(c->p, npairs, pairbuf, slots, grid, d_zres, d_status, st));
     return PNAMP_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Uneven batches in one persistent launch (several contexts: model spaces,
+// meshes, placements). The plan owns its per-context pair records, scratch,
+// work list and device copies of the contexts' parameters; launching only
+// enqueues kernels and a memset, so it can be captured in a CUDA graph.
+struct pnamp_multi {
+    int nctx = 0, form = 0, nitems = 0, grab = 1, grid = 0, grid_max = 0, smem = 0, order = 1;
+    int nsm = 0, optin = 0, grid_req = 0;
+    long long stride = 0, scratch_elems = 0;
+    std::vector<pnamp_ctx *> ctxs;
+    std::vector<int> npairs;
+    std::vector<const double *> uv;
+    std::vector<double *> pairbuf;
+    MultiArgs args{};
+    int4 *d_items = nullptr;
+    zc *scratch = nullptr;
+    int *counter = nullptr;
+};
+
+extern "C" {
+
+void pnamp_multi_free(pnamp_multi *m) {
+    if (!m) return;
+    for (double *q : m->pairbuf) if (q) cudaFree(q);
+    for (void *q : {(void *)m->d_items, (void *)m->scratch, (void *)m->counter})
+        if (q) cudaFree(q);
+    delete m;
+}
+
+int pnamp_multi_schedule(pnamp_multi *m, int order, int grab, int grid) {
+    if (!m || order < 0 || order > 2 || grab < 1 || grab > 64 || grid < 0) return PNAMP_ERR_ARG;
+    std::vector<int4> items;
+    std::vector<int> cidx(m->nctx);
+    for (int c = 0; c < m->nctx; ++c) cidx[c] = c;
+    auto cost = [&](int c) {  // per item: gauge points x n^3
+        const Params &p = m->ctxs[c]->p;
+        return (double)p.n_gauge * p.n * p.n * p.n;
+    };
+    if (order == 1) std::stable_sort(cidx.begin(), cidx.end(), [&](int a, int b) { return cost(a) > cost(b); });
+    if (order == 2) {  // round robin over contexts, item by item
+        std::vector<long long> pos(m->nctx, 0);
+        bool more = true;
+        while (more) {
+            more = false;
+            for (int c = 0; c < m->nctx; ++c) {
+                const long long tot = (long long)m->npairs[c] * m->ctxs[c]->p.n_euler;
+                if (pos[c] < tot) {
+                    const long long k = pos[c]++;
+                    items.push_back(make_int4(c, (int)(k / m->ctxs[c]->p.n_euler), (int)(k % m->ctxs[c]->p.n_euler), 0));
+                    more = true;
+                }
+            }
+        }
+    } else {
+        for (int c : cidx)
+            for (int q = 0; q < m->npairs[c]; ++q)
+                for (int e = 0; e < m->ctxs[c]->p.n_euler; ++e) items.push_back(make_int4(c, q, e, 0));
+    }
+    if ((int)items.size() != m->nitems) return PNAMP_ERR_STATE;
+    CK(cudaMemcpy(m->d_items, items.data(), items.size() * sizeof(int4), cudaMemcpyHostToDevice));
+    m->order = order;
+    m->grab = grab;
+    m->grid_req = grid;
+    m->grid = grid == 0 ? m->grid_max : std::min(grid, m->grid_max);
+    return PNAMP_OK;
+}
+
+int pnamp_multi_placement(pnamp_multi *m, int smem_budget, int *smem_out) {
+    if (!m || smem_budget < 0) return PNAMP_ERR_ARG;
+    const int cap = m->optin - kMultiSmemTail;
+    const int budget = smem_budget == 0 ? cap : std::min(smem_budget, cap);
+    // each context's arrays under the same budget; the launch holds the largest
+    MultiArgs a = m->args;
+    int smem = 0;
+    long long stride = 0;
+    for (int c = 0; c < m->nctx; ++c) {
+        Params q = m->ctxs[c]->p;
+        if (plan_placement(q, budget) != PNAMP_OK) return PNAMP_ERR_UNSUPPORTED;
+        a.p[c] = q;
+        smem = std::max(smem, (q.place.smem_bytes + 15) & ~15);
+        stride = std::max(stride, q.place.slot_elems);
+    }
+    for (int c = m->nctx; c < kMultiCtx; ++c) a.p[c] = a.p[0];
+    a.slot_stride = stride;
+    smem += kMultiSmemTail;
+    int per_sm = 0;
+    if (multi_blocks_per_sm(m->form, smem, &per_sm) != cudaSuccess || per_sm < 1) return PNAMP_ERR_CUDA;
+    const int grid_max = m->nsm * per_sm;
+    if ((long long)grid_max * stride > m->scratch_elems) {
+        if (m->scratch) cudaFree(m->scratch);
+        m->scratch = nullptr;
+        m->scratch_elems = 0;
+        if (cudaMalloc(&m->scratch, (size_t)grid_max * stride * sizeof(zc)) != cudaSuccess) return PNAMP_ERR_NOMEM;
+        m->scratch_elems = (long long)grid_max * stride;
+    }
+    m->args = a;
+    m->smem = smem;
+    m->stride = stride;
+    m->grid_max = grid_max;
+    m->grid = m->grid_req == 0 ? grid_max : std::min(m->grid_req, grid_max);
+    if (smem_out) *smem_out = smem;
+    return PNAMP_OK;
+}
+
+int pnamp_multi_create(int nctx, pnamp_ctx *const *ctxs, const int *npairs, const double *const *d_uv,
+                       double *const *d_zres, int *const *d_status, pnamp_multi **out) {
+    if (!out || nctx < 1 || !ctxs || !npairs || !d_uv || !d_zres || !d_status) return PNAMP_ERR_ARG;
+    *out = nullptr;
+    if (nctx > kMultiCtx) return PNAMP_ERR_UNSUPPORTED;
+    pnamp_multi *m = new pnamp_multi();
+    m->nctx = nctx;
+    m->form = ctxs[0] ? ctxs[0]->p.form : 0;
+    long long nitems = 0;
+    for (int c = 0; c < nctx; ++c) {
+        if (!ctxs[c] || npairs[c] < 1 || !d_uv[c] || !d_zres[c] || !d_status[c] || ctxs[c]->p.form != m->form) {
+            pnamp_multi_free(m);
+            return PNAMP_ERR_ARG;
+        }
+        m->ctxs.push_back(ctxs[c]);
+        m->npairs.push_back(npairs[c]);
+        m->uv.push_back(d_uv[c]);
+        m->args.p[c] = ctxs[c]->p;
+        m->args.zres[c] = d_zres[c];
+        m->args.status[c] = d_status[c];
+        nitems += (long long)npairs[c] * ctxs[c]->p.n_euler;
+        double *pb = nullptr;
+        if (cudaMalloc(&pb, (size_t)npairs[c] * ctxs[c]->p.pl.stride * sizeof(double)) != cudaSuccess) {
+            pnamp_multi_free(m);
+            return PNAMP_ERR_NOMEM;
+        }
+        m->pairbuf.push_back(pb);
+        m->args.pairbuf[c] = pb;
+    }
+    for (int c = nctx; c < kMultiCtx; ++c) {   // unused slots: copies of context 0, never dispatched
+        m->args.pairbuf[c] = m->args.pairbuf[0];
+        m->args.zres[c] = m->args.zres[0];
+        m->args.status[c] = m->args.status[0];
+    }
+    if (nitems > 0x7fffffffLL) {
+        pnamp_multi_free(m);
+        return PNAMP_ERR_UNSUPPORTED;
+    }
+    m->nitems = (int)nitems;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&m->nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&m->optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+        pnamp_multi_free(m);
+        return PNAMP_ERR_CUDA;
+    }
+    if (cudaMalloc(&m->d_items, (size_t)m->nitems * sizeof(int4)) != cudaSuccess ||
+        cudaMalloc(&m->counter, sizeof(int)) != cudaSuccess) {
+        pnamp_multi_free(m);
+        return PNAMP_ERR_NOMEM;
+    }
+    int rc0 = pnamp_multi_placement(m, 0, nullptr);
+    if (rc0) {
+        pnamp_multi_free(m);
+        return rc0;
+    }
+    const int rc = pnamp_multi_schedule(m, 1, 1, 0);
+    if (rc) {
+        pnamp_multi_free(m);
+        return rc;
+    }
+    *out = m;
+    return PNAMP_OK;
+}
+
+int pnamp_multi_launch(pnamp_multi *m, void *stream) {
+    if (!m) return PNAMP_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
+    for (int c = 0; c < m->nctx; ++c) CK(launch_setup(m->ctxs[c]->p, m->npairs[c], m->uv[c], m->pairbuf[c], st));
+    CK(launch_multi(m->form, m->args, m->d_items, m->nitems, m->grab, m->counter, m->scratch, m->grid, m->smem,
+                    st));
+    return PNAMP_OK;
+}
+
+int pnamp_multi_items(const pnamp_multi *m) { return m ? m->nitems : -1; }
+
+}  // extern "C"

@@ -18,6 +18,7 @@ constexpr int kNTrace = 10;              // proton traces of Q_{2mu} rho and Q_{
 constexpr int kNJKK = 1 + 25 + 81 + 169; // (J, K1, K2) with even J <= 6
 constexpr int kProjFields = 5;           // njkk, hjkk, nn, zz, j2
 constexpr int kSetupThreads = 256;
+constexpr int kMultiSmemTail = 16;       // dynamic shared bytes after the placement: multi kernel's counter
 
 // One pair record (doubles), all matrices row-major n x n:
 // U0 V0 U1 V1 W Z0 then [det0, det1, status-as-double, pad].
@@ -80,6 +81,16 @@ struct Params {
     Placement place;
 };
 
+// Contexts of one multi-context launch, passed by value (kernel parameter space).
+constexpr int kMultiCtx = 4;
+struct MultiArgs {
+    Params p[kMultiCtx];
+    const double *pairbuf[kMultiCtx];
+    double *zres[kMultiCtx];
+    int *status[kMultiCtx];
+    long long slot_stride;     // complex elements of one CTA's global slot
+};
+
 // launchers (pnamp_kernels.cu)
 cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *pairbuf,
                          cudaStream_t st);
@@ -91,8 +102,12 @@ cudaError_t launch_project(const Params &p, int npairs, const zc *w, const doubl
 cudaError_t launch_project_q(const Params &p, int axial, int npairs, const double *zres, const double *tj,
                              int exchange, double *out, cudaStream_t st);
 int n_q_outputs();
+cudaError_t multi_blocks_per_sm(int form, int smem_bytes, int *per_sm);
+cudaError_t launch_multi(int form, const MultiArgs &a, const int4 *items, int nitems, int grab, int *counter,
+                         zc *scratch, int grid, int smem, cudaStream_t st);
 cudaError_t set_point_smem(int form, int bytes);
 cudaError_t point_blocks_per_sm(int form, int smem_bytes, int *per_sm);
 int setup_smem_bytes(int n);
+cudaError_t prepare_setup(int n);
 
 }  // namespace pnamp

@@ -372,13 +372,30 @@ setup_kernel(Params p, const double *__restrict__ uv, double *__restrict__ pairb
 
 int setup_smem_bytes(int n) { return (2 * n * n + n + 64) * 8 + (n + 8) * 4; }
 
+// The dynamic shared-memory limit of a kernel is a property of the function,
+// shared by every context on the device: it is raised to the device maximum
+// (never lowered to one context's need), so a context created later cannot
+// invalidate the launches of an earlier one with a larger placement.
+static cudaError_t raise_smem_limit(const void *f) {
+    int dev = 0, optin = 0;
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, f);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    return e;
+}
+
+cudaError_t prepare_setup(int n) {
+    if (setup_smem_bytes(n) <= 48 * 1024) return cudaSuccess;
+    return raise_smem_limit((const void *)setup_kernel);
+}
+
+// Enqueues only (no attribute calls): usable under stream capture once
+// prepare_setup(n) ran at context creation.
 cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *pairbuf, cudaStream_t st) {
-    const int smem = setup_smem_bytes(p.n);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(setup_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-    }
-    setup_kernel<<<npairs, kSetupThreads, smem, st>>>(p, uv, pairbuf);
+    setup_kernel<<<npairs, kSetupThreads, setup_smem_bytes(p.n), st>>>(p, uv, pairbuf);
     return cudaGetLastError();
 }
 
@@ -392,10 +409,14 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// One work item: Euler point `ie` of pair `pair`, all its gauge points, in the
+// CTA's workspace `slot`. `reload` is set when the previous item of this CTA
+// belonged to another pair (or context): V0^T, U0^T and the phase tables are
+// then (re)loaded.
 template <class Z>
-__global__ void __launch_bounds__(kThreads, 1)
-point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scratch,
-             double *__restrict__ zres, int *__restrict__ status) {
+__device__ __forceinline__ void point_item(const Params &p, const double *__restrict__ pairbuf, zc *slot,
+                                           int pair, int ie, bool reload, double *__restrict__ zres,
+                                           int *__restrict__ status) {
     using A = Ar<Z>;
     using R = typename A::R;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -404,7 +425,6 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
     const int ld = n + 1;  // density row stride: transposed reads stay bank-conflict free
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const Placement &pl = p.place;
-    zc *slot = scratch + (long long)blockIdx.x * pl.slot_elems;
     Z *X = reinterpret_cast<Z *>(slot + pl.g_x);    // R W R^T
     Z *B = reinterpret_cast<Z *>(slot + pl.g_b);    // rows 0..n-1: R V1, rows n..2n-1: conj(R) U1
     zc *Bz = slot + pl.g_b;                         // the same storage while it holds FP64 values
@@ -429,15 +449,7 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
     Z *Kc = S + 3 * n * ld;  // antisymmetrised pairing tensors
 
     const double twopi = 6.283185307179586476925287;
-    for (int l = threadIdx.x; l < p.nfom; l += blockDim.x) {
-        const zc e = expi(p.nfom == 1 ? 0.0 : twopi * l / p.nfom);
-        eph[l] = e;
-        ephz[l] = A::from(e);
-    }
-    const long long total = (long long)npairs * p.n_euler;
-    int cur_pair = -1;
-    for (long long item = blockIdx.x; item < total; item += gridDim.x) {
-        const int pair = (int)(item / p.n_euler), ie = (int)(item % p.n_euler);
+    {
         const double *pr = pairbuf + (long long)pair * p.pl.stride;
         const double *gU1 = pr + p.pl.u1, *gV1 = pr + p.pl.v1, *gU0 = pr + p.pl.u0, *gV0 = pr + p.pl.v0;
         const double *gW = pr + p.pl.w, *gZ0 = pr + p.pl.z0;
@@ -450,16 +462,20 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
                 zout[2LL * (io * p.n_euler + ie) + 1] = 0.0;
             }
             if (threadIdx.x == 0) status[(long long)pair * p.n_euler + ie] = 8;
-            continue;
+            return;
         }
-        if (pair != cur_pair) {
+        if (reload) {
             __syncthreads();
             for (int t = threadIdx.x; t < nn; t += blockDim.x) {
                 const int k = t / n, j = t % n;
                 V0t[t] = A::real(gV0[j * n + k]);
                 U0t[t] = A::real(gU0[j * n + k]);
             }
-            cur_pair = pair;
+            for (int l = threadIdx.x; l < p.nfom; l += blockDim.x) {
+                const zc e = expi(p.nfom == 1 ? 0.0 : twopi * l / p.nfom);
+                eph[l] = e;
+                ephz[l] = A::from(e);
+            }
         }
         // ---- rotation blocks R_b(i,k) = e^{-i alp m_i} d^j_{m_i m_k}(bet) e^{-i gam m_k}  (FP64)
         const double alp = p.euler[4 * ie], bet = p.euler[4 * ie + 1], gam = p.euler[4 * ie + 2];
@@ -805,8 +821,92 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
 }
 
 template <class Z>
+__global__ void __launch_bounds__(kThreads, 1)
+point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scratch,
+             double *__restrict__ zres, int *__restrict__ status) {
+    zc *slot = scratch + (long long)blockIdx.x * p.place.slot_elems;
+    const long long total = (long long)npairs * p.n_euler;
+    int cur_pair = -1;
+    for (long long item = blockIdx.x; item < total; item += gridDim.x) {
+        const int pair = (int)(item / p.n_euler), ie = (int)(item % p.n_euler);
+        point_item<Z>(p, pairbuf, slot, pair, ie, pair != cur_pair, zres, status);
+        cur_pair = pair;
+    }
+}
+
+// Persistent kernel over an uneven batch: work items (context, pair, Euler point)
+// of up to kMultiCtx contexts (model spaces, meshes, placements), taken `grab`
+// at a time from a global counter in the order of `items` (set by the schedule).
+// Every context's parameters travel by value in the launch's parameter space and
+// each context has its own inlined copy of the point body, so the per-point code
+// reads its sizes and table pointers as constant-bank operands exactly as the
+// single-context kernel does (an indexed parameter array would become a load per
+// use inside the hot loops).
+template <class Z>
+__device__ __forceinline__ void multi_item(const MultiArgs &a, int4 m, zc *slot, bool reload) {
+    switch (m.x) {
+    case 0: point_item<Z>(a.p[0], a.pairbuf[0], slot, m.y, m.z, reload, a.zres[0], a.status[0]); break;
+    case 1: point_item<Z>(a.p[1], a.pairbuf[1], slot, m.y, m.z, reload, a.zres[1], a.status[1]); break;
+    case 2: point_item<Z>(a.p[2], a.pairbuf[2], slot, m.y, m.z, reload, a.zres[2], a.status[2]); break;
+    default: point_item<Z>(a.p[3], a.pairbuf[3], slot, m.y, m.z, reload, a.zres[3], a.status[3]); break;
+    }
+}
+static_assert(kMultiCtx == 4, "multi_item dispatches four contexts");
+
+template <class Z>
+__global__ void __launch_bounds__(kThreads, 1)
+multi_point_kernel(const __grid_constant__ MultiArgs a, const int4 *__restrict__ items, int nitems, int grab,
+                   zc *scratch, int *counter, int smem_tail) {
+    // the work counter's broadcast lives past every context's placement (no static
+    // shared memory, so the dynamic limit can be the device maximum)
+    extern __shared__ __align__(16) unsigned char smem_all[];
+    int &s_next = *reinterpret_cast<int *>(smem_all + smem_tail);
+    zc *slot = scratch + (long long)blockIdx.x * a.slot_stride;
+    int cur_ctx = -1, cur_pair = -1;
+    for (;;) {
+        if (threadIdx.x == 0) s_next = atomicAdd(counter, grab);
+        __syncthreads();
+        const int base = s_next;
+        __syncthreads();
+        if (base >= nitems) break;
+        const int end = min(base + grab, nitems);
+        for (int it = base; it < end; ++it) {
+            const int4 m = items[it];  // (context, pair, Euler point, unused)
+            multi_item<Z>(a, m, slot, m.x != cur_ctx || m.y != cur_pair);
+            cur_ctx = m.x;
+            cur_pair = m.y;
+        }
+    }
+}
+
+template <class Z>
 static const void *point_fn() {
     return reinterpret_cast<const void *>(point_kernel<Z>);
+}
+
+template <class Z>
+static const void *multi_fn() {
+    return reinterpret_cast<const void *>(multi_point_kernel<Z>);
+}
+
+cudaError_t multi_blocks_per_sm(int form, int smem_bytes, int *per_sm) {
+    const void *f = form == 1 ? multi_fn<zd>() : multi_fn<zc>();
+    cudaError_t e = raise_smem_limit(f);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, f, kThreads, smem_bytes);
+}
+
+cudaError_t launch_multi(int form, const MultiArgs &a, const int4 *items, int nitems, int grab, int *counter,
+                         zc *scratch, int grid, int smem, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    if (form == 1)
+        multi_point_kernel<zd><<<grid, kThreads, smem, st>>>(a, items, nitems, grab, scratch, counter,
+                                                            smem - kMultiSmemTail);
+    else
+        multi_point_kernel<zc><<<grid, kThreads, smem, st>>>(a, items, nitems, grab, scratch, counter,
+                                                            smem - kMultiSmemTail);
+    return cudaGetLastError();
 }
 
 cudaError_t point_blocks_per_sm(int form, int smem_bytes, int *per_sm) {
@@ -815,8 +915,8 @@ cudaError_t point_blocks_per_sm(int form, int smem_bytes, int *per_sm) {
 }
 
 cudaError_t set_point_smem(int form, int bytes) {
-    return cudaFuncSetAttribute(form == 1 ? point_fn<zd>() : point_fn<zc>(),
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    (void)bytes;  // checked against the device maximum by the placement planner
+    return raise_smem_limit(form == 1 ? point_fn<zd>() : point_fn<zc>());
 }
 
 cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc *scratch, int grid,

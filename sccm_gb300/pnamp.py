@@ -43,7 +43,8 @@ _lib = None
 EXPORTS = ("pnamp_init", "pnamp_n_euler", "pnamp_pair", "pnamp_batch", "pnamp_batch_device",
            "pnamp_project", "pnamp_project_device", "pnamp_sync", "pnamp_free",
            "pnamp_strerror", "pnamp_version", "pnamp_batch_device_noalloc", "pnamp_set_form",
-           "pnamp_project_q", "pnamp_project_q_device")
+           "pnamp_project_q", "pnamp_project_q_device", "pnamp_multi_create", "pnamp_multi_schedule",
+           "pnamp_multi_launch", "pnamp_multi_items", "pnamp_multi_free", "pnamp_multi_placement")
 FORMS = {"fp64": 0, "df64": 1}
 PNAMP_ERR_SCRATCH_LIMIT = 7
 
@@ -105,6 +106,14 @@ def load_library(path: str | None = None):
     lib.pnamp_project_q.argtypes = [vp, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_double),
                                     C.POINTER(C.c_double)]
     lib.pnamp_project_q_device.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp]
+    lib.pnamp_multi_create.argtypes = [C.c_int, C.POINTER(vp), C.POINTER(C.c_int), C.POINTER(vp),
+                                       C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]
+    lib.pnamp_multi_schedule.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    lib.pnamp_multi_launch.argtypes = [vp, vp]
+    lib.pnamp_multi_placement.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
+    lib.pnamp_multi_items.argtypes = [vp]
+    lib.pnamp_multi_free.argtypes = [vp]
+    lib.pnamp_multi_free.restype = None
     lib.pnamp_sync.argtypes = [vp]
     lib.pnamp_free.argtypes = [vp]
     lib.pnamp_free.restype = None
@@ -286,6 +295,68 @@ class PnampContext:
         rc = load_library().pnamp_sync(self._h)
         if rc != PNAMP_OK:
             raise PnampError(rc, "pnamp_sync")
+
+
+class MultiPlan:
+    """Several contexts' pair batches in one persistent launch (`pnamp_multi_*`).
+
+    `parts` is a list of (ctx, npairs, d_uv, d_zres, d_status) with device
+    addresses (ints) the caller keeps alive; results land in each context's
+    own buffers as `batch_device` writes them ([npairs][NOBS][P_E] complex,
+    [npairs][P_E] status). All contexts must be in the same form.
+    """
+
+    def __init__(self, parts):
+        lib = load_library()
+        k = len(parts)
+        vp = C.c_void_p
+        hs = (vp * k)(*[p[0]._h for p in parts])
+        nps = (C.c_int * k)(*[int(p[1]) for p in parts])
+        uvs = (vp * k)(*[p[2] for p in parts])
+        zs = (vp * k)(*[p[3] for p in parts])
+        sts = (vp * k)(*[p[4] for p in parts])
+        h = vp()
+        rc = lib.pnamp_multi_create(k, hs, nps, uvs, zs, sts, C.byref(h))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_multi_create")
+        self._h = h
+        self.parts = parts
+        self.nitems = lib.pnamp_multi_items(h)
+        self.schedule_args = (1, 1, 0)
+        self.smem_budget = 0
+        self.smem_bytes = None
+
+    def schedule(self, order=1, grab=1, grid=0):
+        rc = load_library().pnamp_multi_schedule(self._h, order, grab, grid)
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_multi_schedule")
+        self.schedule_args = (order, grab, grid)
+
+    def placement(self, smem_budget=0):
+        """Re-place every context's arrays under `smem_budget` bytes per CTA (0: device maximum)."""
+        out = C.c_int(0)
+        rc = load_library().pnamp_multi_placement(self._h, int(smem_budget), C.byref(out))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_multi_placement")
+        self.smem_budget = int(smem_budget)
+        self.smem_bytes = out.value
+        return out.value
+
+    def launch(self, stream=0):
+        rc = load_library().pnamp_multi_launch(self._h, C.c_void_p(stream))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_multi_launch")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().pnamp_multi_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def kernel4triaxial(ctx: PnampContext, U0, V0, U1, V1, chop=True):

@@ -257,8 +257,26 @@ def make_workload(shell, nvac, mesh: Mesh, seed, name=None, rot_scale=0.3, defor
 def config(idx, small=False):
     """Benchmark configurations (mesh sizes as quoted; `small` shrinks the vacuum count)."""
     if idx == 0:
-        return make_workload("sd", 2, Mesh(8, 16, 8, 7), seed=1000, name="cfg0-sd", deformed=False)
+        return make_workload("sd", 2, Mesh(8, 16, 8, 7), seed=1000, name="sd-2vac-8x16x8-g7", deformed=False)
     if idx in (1, 2):
         return make_workload("pf", 4 if small else 20, Mesh(10, 20, 10, 9), seed=2000,
-                             name="cfg1-pf" if idx == 1 else "cfg2-pf-bf16x3")
+                             name="pf-20vac-10x20x10-g9")
     raise ValueError(f"unknown configuration {idx}")
+
+
+def uneven_workloads(scale=1):
+    """The uneven batch: 64 sd pairs (mesh 8x16x8, gauge 7x7), 128 pf pairs
+    (10x20x10, 9x9) and 16 sd+pf cross-shell pairs (n = 64, 12x24x12, 11x11).
+
+    Each part has its own seeded vacua and interaction; the pair lists are the
+    first pairs (i <= j) of 11, 16 and 6 vacua. `scale` > 1 divides the pair
+    counts (at least one pair per part) for smaller runs of the same mix.
+    """
+    parts = []
+    for shell, nvac, npairs, mesh, seed in (("sd", 11, 64, Mesh(8, 16, 8, 7), 3000),
+                                            ("pf", 16, 128, Mesh(10, 20, 10, 9), 3100),
+                                            ("sdpf", 6, 16, Mesh(12, 24, 12, 11), 3200)):
+        wl = make_workload(shell, nvac, mesh, seed=seed, name=f"uneven-{shell}")
+        wl.pairs = wl.pairs[:max(1, npairs // scale)]
+        parts.append(wl)
+    return parts
