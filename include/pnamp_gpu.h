@@ -113,6 +113,16 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h,
  * No counterpart in the reference, which computes in FP64 only. */
 int pnamp_set_form(pnamp_ctx *ctx, int form);
 
+/* Outputs of later pair/batch calls: PNAMP_OUT_ALL (default) computes the 19
+ * observables of ZRES; PNAMP_OUT_NORM only the norm kernel N(Omega) (column
+ * io = 0; the other columns are written as 0), skipping T22, the densities
+ * and the energy. No counterpart in the reference, which always evaluates
+ * everything at every point; the learned mode needs the exact norm on the
+ * whole fine mesh and the rest only where it computes points exactly. */
+#define PNAMP_OUT_ALL 0
+#define PNAMP_OUT_NORM 1
+int pnamp_set_outputs(pnamp_ctx *ctx, int outputs);
+
 /* Number of Euler points P_E of the context's mesh (rows of ZRES). */
 int pnamp_n_euler(const pnamp_ctx *ctx);
 
@@ -134,6 +144,21 @@ int pnamp_batch(pnamp_ctx *ctx, int npairs, const double *uv, double *zres, int 
  * cudaStream_t, NULL = legacy default stream); returns after the launch. */
 int pnamp_batch_device(pnamp_ctx *ctx, int npairs, const double *d_uv,
                        double *d_zres, int *d_point_status, void *stream);
+
+/* pnamp_batch_device restricted to listed Euler points: d_items holds nitems
+ * (pair, Euler point) int pairs (0-based); only those entries of d_zres and
+ * d_point_status ([npairs][NOBS][P_E] complex, [npairs][P_E]) are written.
+ * d_gauge_out, when not NULL, receives per gauge point (phi_p outer, phi_n
+ * inner) [npairs][P_E][NFOM*NFOM][4] doubles: the norm N(Omega, phi) with its
+ * gauge phase (complex) and H/N at that point (complex; 0 when only the norm
+ * was computed or T22 was singular), so that ZRES(ie, 1) is the mean of the
+ * first and ZRES(ie, 7) the mean of their products. Items with a pair index
+ * outside [0, npairs) or an Euler index outside [0, P_E) are skipped (nothing
+ * written). No reference counterpart (the reference always sweeps the whole
+ * mesh). */
+int pnamp_batch_items_device(pnamp_ctx *ctx, int npairs, const double *d_uv,
+                             long long nitems, const int *d_items, double *d_zres,
+                             int *d_point_status, double *d_gauge_out, void *stream);
 
 /* Same computation as pnamp_batch_device, for callers that must not allocate
  * device memory per call: code running under a runtime that owns the device

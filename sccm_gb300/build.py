@@ -2,7 +2,8 @@
 
 Plain nvcc, one -gencode, the translation units compiled in parallel and
 linked with -shared. No cmake, no torch extension machinery: the library's
-boundary is a C ABI (include/pnamp_gpu.h) and it links only the CUDA runtime.
+boundary is a C ABI (include/pnamp_gpu.h, include/pnamp_mlp.h) and it links only
+the CUDA runtime.
 """
 from __future__ import annotations
 
@@ -17,7 +18,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libpnamp_gb300.so")
-SOURCES = ["pnamp_kernels.cu", "pnamp_capi.cu"]
+SOURCES = ["pnamp_kernels.cu", "pnamp_capi.cu", "mlp_kernels.cu", "learned_kernels.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -30,7 +31,8 @@ def nvcc_path() -> str:
 
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files.append(os.path.join(ROOT, "include", "pnamp_gpu.h"))
+    inc = os.path.join(ROOT, "include")
+    files += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
     return files
 
 

@@ -216,6 +216,12 @@ int pnamp_set_form(pnamp_ctx *ctx, int form) {
     return PNAMP_OK;
 }
 
+int pnamp_set_outputs(pnamp_ctx *ctx, int outputs) {
+    if (!ctx || (outputs != PNAMP_OUT_ALL && outputs != PNAMP_OUT_NORM)) return PNAMP_ERR_ARG;
+    ctx->p.norm_only = outputs == PNAMP_OUT_NORM ? 1 : 0;
+    return PNAMP_OK;
+}
+
 void pnamp_free(pnamp_ctx *ctx) {
     if (!ctx) return;
     for (void *q : ctx->allocs) cudaFree(q);
@@ -416,6 +422,7 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
         c->grid_form[form] = nsm * per_sm;
     }
     p.form = 0;
+    p.norm_only = 0;
     c->grid = std::max(c->grid_form[0], c->grid_form[1]);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         pnamp_free(c);
@@ -462,6 +469,21 @@ int pnamp_batch_device(pnamp_ctx *c, int npairs, const double *d_uv, double *d_z
     cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
     CK(launch_setup(c->p, npairs, d_uv, c->d_pairbuf, st));
     CK(launch_points(c->p, npairs, c->d_pairbuf, c->d_scratch, c->grid_form[c->p.form], d_zres, d_status, st));
+    return PNAMP_OK;
+}
+
+int pnamp_batch_items_device(pnamp_ctx *c, int npairs, const double *d_uv, long long nitems, const int *d_items,
+                             double *d_zres, int *d_status, double *d_gauge_out, void *stream) {
+    if (!c || npairs < 0 || nitems < 0 || (nitems > 0 && (npairs == 0 || !d_uv || !d_items || !d_zres || !d_status)))
+        return PNAMP_ERR_ARG;
+    if (nitems == 0) return PNAMP_OK;
+    int rc = ensure_pairs(c, npairs);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
+    CK(launch_setup(c->p, npairs, d_uv, c->d_pairbuf, st));
+    const int grid = (int)std::min<long long>(c->grid_form[c->p.form], nitems);
+    CK(launch_points(c->p, npairs, c->d_pairbuf, c->d_scratch, grid, d_zres, d_status, st,
+                     reinterpret_cast<const int2 *>(d_items), nitems, d_gauge_out));
     return PNAMP_OK;
 }
 

@@ -66,6 +66,7 @@ struct Params {
     double vacfac;             // (-1)^{n(n+1)/2} * 10^(-2*(n*iscale/2))
     int iE2;
     int form;                  // 0: FP64 (plain), 1: double-float per-point algebra
+    int norm_only;             // 1: only the norm kernel N(Omega) (observable 0); the others are 0
     // rotation blocks
     int nblk, rot_elems;
     const int *blk_start, *blk_size, *blk_tj, *blk_roff, *row_blk, *twom;
@@ -95,7 +96,8 @@ struct MultiArgs {
 cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *pairbuf,
                          cudaStream_t st);
 cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc *scratch,
-                          int grid, double *zres, int *status, cudaStream_t st);
+                          int grid, double *zres, int *status, cudaStream_t st,
+                          const int2 *items = nullptr, long long nitems = 0, double *gout = nullptr);
 cudaError_t launch_proj_weights(const Params &p, int axial, zc *w, cudaStream_t st);
 cudaError_t launch_project(const Params &p, int npairs, const zc *w, const double *zres,
                            int core_prot, int core_neut, int chop, double *out, cudaStream_t st);

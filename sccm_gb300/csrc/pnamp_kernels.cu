@@ -416,7 +416,7 @@ __device__ __forceinline__ double warp_sum(double v) {
 template <class Z>
 __device__ __forceinline__ void point_item(const Params &p, const double *__restrict__ pairbuf, zc *slot,
                                            int pair, int ie, bool reload, double *__restrict__ zres,
-                                           int *__restrict__ status) {
+                                           int *__restrict__ status, double *__restrict__ gout = nullptr) {
     using A = Ar<Z>;
     using R = typename A::R;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -524,7 +524,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
             for (int k = 0; k < d; ++k) x = zfma(RW[a * n + s0 + k], Rr[k], x);
             X[t] = A::from(x);
         }
-        for (int t = threadIdx.x; t < 4 * nn; t += blockDim.x) {
+        for (int t = threadIdx.x; t < (p.norm_only ? 0 : 4 * nn); t += blockDim.x) {
             const int q = t / nn, e = t % nn, i = e / n, j = e % n;
             const double *M = (q < 2) ? gV0 : gU0;
             const zc *Bq = (q < 2) ? Bz : Bz + nn;
@@ -534,7 +534,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
             P[t] = A::from(s);
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) {  // in place, element by element
+        for (int t = threadIdx.x; t < (p.norm_only ? 0 : 2 * nn); t += blockDim.x) {  // in place
             const zc v = Bz[t];
             B[t] = A::from(v);
         }
@@ -599,6 +599,9 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 } else {
                     pf = pfaffian_upper<Z>(S, N, vec, red, sh + 2, under);
                 }
+                bool sing = false;
+                double *fin = red, *pw = red + kNSlot + 2;
+                if (!p.norm_only) {  // uniform over the block: norm-only launches skip the densities
                 // ---- T22(phi) and right-hand sides
                 for (int t = threadIdx.x; t < nn; t += blockDim.x) {
                     Z s = zep * P[t];
@@ -609,7 +612,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 }
                 for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) Y[t] = B[t];
                 __syncthreads();
-                const bool sing = lu_factor<Z>(T, n, n, perm, invd, sh);
+                sing = lu_factor<Z>(T, n, n, perm, invd, sh);
                 row_solve<Z>(Y, 2 * n, n, T, n, n, perm, invd);
                 // ---- densities into the Pfaffian's storage, row stride ld
                 {
@@ -646,7 +649,6 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 __syncthreads();
                 // ---- observables. Final sums land in red[0..kNSlot); the energy and <J^2>
                 // sums, spread over all warps, leave per-warp partials in red[kNSlot + ..].
-                double *fin = red, *pw = red + kNSlot + 2;
                 if (wid == 0) {  // traces of rho: warp 0 alone
                     double z0 = 0, z1 = 0, n0 = 0, n1 = 0, j0 = 0, j1 = 0, p0 = 0, p1 = 0, m0 = 0, m1 = 0, c0 = 0,
                            c1 = 0, t0 = 0, t1 = 0;
@@ -768,6 +770,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     put(2, rc.x);
                     put(3, rc.y);
                 }
+                }  // !norm_only
                 __syncthreads();
                 if (threadIdx.x == 0) {
                     auto get = [&](int slot) {
@@ -784,14 +787,24 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     const zc j2 = mk(get(16) + get(8), get(17) + get(9)) + trp * trm + trz * trz;
                     const zc ekin = mk(get(4), get(5));
                     acc[0] = acc[0] + norm;
+                    zc hg = mk(0.0, 0.0);  // H/N at this gauge point (0 when not computed)
+                    if (!p.norm_only && !sing) hg = ekin + mk(get(6), get(7)) + mk(p.e0, 0.0);
+                    if (gout) {  // per gauge point: N (with the gauge phase) and H/N
+                        double *g = gout + 4LL * (((long long)pair * p.n_euler + ie) * p.n_gauge + lp * p.nfom + ln);
+                        g[0] = norm.x;
+                        g[1] = norm.y;
+                        g[2] = hg.x;
+                        g[3] = hg.y;
+                    }
                     int f = (under == 1) ? 1 : (under == 2 ? 4 : 0);
-                    if (sing) {
+                    if (p.norm_only) {
+                    } else if (sing) {
                         f |= 2;
                     } else {
                         acc[1] = zfma(norm, mk(get(0), get(1)), acc[1]);
                         acc[2] = zfma(norm, mk(get(2), get(3)), acc[2]);
                         acc[3] = zfma(norm, ekin, acc[3]);
-                        acc[6] = zfma(norm, ekin + mk(get(6), get(7)) + mk(p.e0, 0.0), acc[6]);
+                        acc[6] = zfma(norm, hg, acc[6]);
                         acc[7] = zfma(norm, j2, acc[7]);
                         if (p.iE2)
                             for (int q = 0; q < 5; ++q) {
@@ -823,13 +836,24 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
 template <class Z>
 __global__ void __launch_bounds__(kThreads, 1)
 point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scratch,
-             double *__restrict__ zres, int *__restrict__ status) {
+             double *__restrict__ zres, int *__restrict__ status, const int2 *__restrict__ items,
+             long long nitems, double *__restrict__ gout) {
+    // items == nullptr: every (pair, Euler point) of the batch; else the listed (pair, ie)
     zc *slot = scratch + (long long)blockIdx.x * p.place.slot_elems;
-    const long long total = (long long)npairs * p.n_euler;
+    const long long total = items ? nitems : (long long)npairs * p.n_euler;
     int cur_pair = -1;
     for (long long item = blockIdx.x; item < total; item += gridDim.x) {
-        const int pair = (int)(item / p.n_euler), ie = (int)(item % p.n_euler);
-        point_item<Z>(p, pairbuf, slot, pair, ie, pair != cur_pair, zres, status);
+        int pair, ie;
+        if (items) {
+            const int2 it = items[item];
+            pair = it.x;
+            ie = it.y;
+            if (pair < 0 || pair >= npairs || ie < 0 || ie >= p.n_euler) continue;  // out of range: skipped
+        } else {
+            pair = (int)(item / p.n_euler);
+            ie = (int)(item % p.n_euler);
+        }
+        point_item<Z>(p, pairbuf, slot, pair, ie, pair != cur_pair, zres, status, gout);
         cur_pair = pair;
     }
 }
@@ -920,11 +944,14 @@ cudaError_t set_point_smem(int form, int bytes) {
 }
 
 cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc *scratch, int grid,
-                          double *zres, int *status, cudaStream_t st) {
+                          double *zres, int *status, cudaStream_t st, const int2 *items, long long nitems,
+                          double *gout) {
     if (p.form == 1)
-        point_kernel<zd><<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status);
+        point_kernel<zd><<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status,
+                                                                    items, nitems, gout);
     else
-        point_kernel<zc><<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status);
+        point_kernel<zc><<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status,
+                                                                    items, nitems, gout);
     return cudaGetLastError();
 }
 

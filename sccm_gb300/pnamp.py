@@ -44,7 +44,8 @@ EXPORTS = ("pnamp_init", "pnamp_n_euler", "pnamp_pair", "pnamp_batch", "pnamp_ba
            "pnamp_project", "pnamp_project_device", "pnamp_sync", "pnamp_free",
            "pnamp_strerror", "pnamp_version", "pnamp_batch_device_noalloc", "pnamp_set_form",
            "pnamp_project_q", "pnamp_project_q_device", "pnamp_multi_create", "pnamp_multi_schedule",
-           "pnamp_multi_launch", "pnamp_multi_items", "pnamp_multi_free", "pnamp_multi_placement")
+           "pnamp_multi_launch", "pnamp_multi_items", "pnamp_multi_free", "pnamp_multi_placement",
+           "pnamp_set_outputs", "pnamp_batch_items_device")
 FORMS = {"fp64": 0, "df64": 1}
 PNAMP_ERR_SCRATCH_LIMIT = 7
 
@@ -96,6 +97,8 @@ def load_library(path: str | None = None):
     lib.pnamp_init.argtypes = [C.POINTER(_Space), C.POINTER(_Ham), C.POINTER(_Mesh), C.POINTER(vp)]
     lib.pnamp_n_euler.argtypes = [vp]
     lib.pnamp_set_form.argtypes = [vp, C.c_int]
+    lib.pnamp_set_outputs.argtypes = [vp, C.c_int]
+    lib.pnamp_batch_items_device.argtypes = [vp, C.c_int, vp, C.c_longlong, vp, vp, vp, vp, vp]
     lib.pnamp_pair.argtypes = [vp] + [C.POINTER(C.c_double)] * 5 + [C.POINTER(C.c_int)]
     lib.pnamp_batch.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_int)]
@@ -278,7 +281,24 @@ class PnampContext:
             raise PnampError(rc, "pnamp_project_q")
         return qp, qc
 
+    def set_outputs(self, outputs):
+        """"all" (19 observables) or "norm" (N(Omega) only) for later batches."""
+        rc = load_library().pnamp_set_outputs(self._h, {"all": 0, "norm": 1}[outputs])
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_set_outputs")
+        self.outputs = outputs
+
     # device-pointer entry points (inputs already resident in HBM)
+    def batch_items_device(self, npairs, d_uv, nitems, d_items, d_zres, d_status, d_gauge=0, stream=0):
+        """Only the listed (pair, Euler point) items; `d_items` is int32 [nitems, 2]; `d_gauge`
+        (optional) receives [npairs][P_E][P_G][N re, N im, H/N re, H/N im] float64."""
+        rc = load_library().pnamp_batch_items_device(self._h, npairs, C.c_void_p(d_uv), int(nitems),
+                                                     C.c_void_p(d_items), C.c_void_p(d_zres),
+                                                     C.c_void_p(d_status), C.c_void_p(d_gauge or None),
+                                                     C.c_void_p(stream))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_batch_items_device")
+
     def batch_device(self, npairs, d_uv, d_zres, d_status, stream=0):
         rc = load_library().pnamp_batch_device(self._h, npairs, C.c_void_p(d_uv), C.c_void_p(d_zres),
                                                C.c_void_p(d_status), C.c_void_p(stream))

@@ -1,4 +1,4 @@
-"""The C-ABI library loads and exports every symbol include/pnamp_gpu.h declares (no GPU calls)."""
+"""The C-ABI library loads and exports every symbol include/*.h declares (no GPU calls)."""
 import ctypes
 import os
 import re
@@ -9,8 +9,9 @@ from conftest import ROOT
 
 
 def declared_symbols():
-    txt = open(os.path.join(ROOT, "include", "pnamp_gpu.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(pnamp_\w+)\s*\(", txt, re.M)))
+    inc = os.path.join(ROOT, "include")
+    txt = "".join(open(os.path.join(inc, f)).read() for f in sorted(os.listdir(inc)) if f.endswith(".h"))
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+(?:\s+\w+)?\s*\*?\s*(pnamp_\w+)\s*\(", txt, re.M)))
 
 
 @pytest.fixture(scope="module")
@@ -31,8 +32,9 @@ def test_library_exports_declared_symbols(lib):
 
 
 def test_python_host_binds_every_export():
+    from sccm_gb300.mlp import MLP_EXPORTS
     from sccm_gb300.pnamp import EXPORTS
-    assert sorted(EXPORTS) == declared_symbols()
+    assert sorted(EXPORTS + MLP_EXPORTS) == declared_symbols()
 
 
 def test_strerror_and_version(lib):
