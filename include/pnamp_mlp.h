@@ -39,9 +39,11 @@ int pnamp_mlp_loss_blocks(int rows);
 /* Heteroscedastic Gaussian loss of outputs out [rows][3] = (mu_re, mu_im,
  * s = log sigma, clamped to [-12, 6]) against targets y [rows][2] with row
  * weights w [rows] (NULL: 1):  mean_r w_r [|y - mu|^2 e^{-2s}/2 + 2s].
- * Writes dout [rows][3] = d loss / d out and per-block partial losses (sum
- * them for the loss). */
-int pnamp_mlp_gauss_loss(const float *out, const float *y, const float *w, int rows,
+ * mode 0: gradients to mu and s; 1: s taken as 0 and left alone (weighted
+ * least squares on mu); 2: gradient to s only (the uncertainty fitted to the
+ * current errors). Writes dout [rows][3] = d loss / d out and per-block
+ * partial losses (sum them for the loss). */
+int pnamp_mlp_gauss_loss(const float *out, const float *y, const float *w, int rows, int mode,
                          float *dout, float *loss_part, void *stream);
 
 /* Adam step (bias-corrected, step >= 1) on n parameters. */

@@ -8,6 +8,7 @@ exactly, Codes/PNAMP/PNAMP_Kernel3D.f90:178-260), so there is no reference
 file to follow; the formulas are the textbook ones:
   * layer: Y = act(X W^T + b), dZ = dY * act'(Z), dW = dZ^T X, db = sum_r dZ, dX = dZ W
   * loss: mean_r w_r [ |y_r - mu_r|^2 e^{-2 s_r} / 2 + 2 s_r ], s clamped to [-12, 6]
+    (mode 1: s = 0 and no gradient to s; mode 2: no gradient to mu)
   * Adam (Kingma & Ba 2015) with bias correction.
 """
 from __future__ import annotations
@@ -38,18 +39,20 @@ def forward(flat, dims, x):
     return acts
 
 
-def gauss_loss(out, y, w=None):
+def gauss_loss(out, y, w=None, mode=0):
+    """mode 0: gradients to mu and s; 1: s = 0, no gradient to s; 2: gradient to s only."""
     rows = out.shape[0]
     w = np.ones(rows) if w is None else np.asarray(w, dtype=np.float64)
     s_raw = out[:, 2]
-    s = np.clip(s_raw, -12.0, 6.0)
+    s = np.zeros(rows) if mode == 1 else np.clip(s_raw, -12.0, 6.0)
     er, ei = y[:, 0] - out[:, 0], y[:, 1] - out[:, 1]
     iv = np.exp(-2.0 * s)
     e2 = er * er + ei * ei
     loss = np.sum(w * (0.5 * e2 * iv + 2.0 * s)) / rows
     g = w / rows
-    dout = np.stack([-g * er * iv, -g * ei * iv,
-                     np.where((s_raw > -12.0) & (s_raw < 6.0), g * (2.0 - e2 * iv), 0.0)], axis=1)
+    ds = np.where((s_raw > -12.0) & (s_raw < 6.0), g * (2.0 - e2 * iv), 0.0)
+    dm = 0.0 if mode == 2 else 1.0
+    dout = np.stack([-g * er * iv * dm, -g * ei * iv * dm, ds * (mode != 1)], axis=1)
     return loss, dout
 
 

@@ -124,25 +124,27 @@ __global__ void colsum_partial(const float *__restrict__ dz, int rows, int out, 
     }
 }
 
-// loss_r = w_r [ |y - mu|^2 e^{-2s} / 2 + 2 s ],  s = clamp(out[2], -12, 6)
-// dout = w_r / rows * [ -(y - mu) e^{-2s},  -|y - mu|^2 e^{-2s} + 2 ]
+// mode 0: loss_r = w_r [ |y - mu|^2 e^{-2s} / 2 + 2 s ],  s = clamp(out[2], -12, 6)
+//         dout = w_r / rows * [ -(y - mu) e^{-2s},  -|y - mu|^2 e^{-2s} + 2 ]
+// mode 1: the same with s = 0 and no gradient to s (weighted least squares on mu)
+// mode 2: the same with no gradient to mu (fits s to the current errors)
 __global__ void gauss_loss(const float *__restrict__ out, const float *__restrict__ y, const float *__restrict__ w,
-                           int rows, float *__restrict__ dout, float *__restrict__ loss_part) {
+                           int rows, int mode, float *__restrict__ dout, float *__restrict__ loss_part) {
     __shared__ float red[256];
     float acc = 0.f;
     const float inv_rows = 1.f / (float)rows;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
         const float mr = out[3 * r], mi = out[3 * r + 1], s_raw = out[3 * r + 2];
-        const float s = fminf(fmaxf(s_raw, -12.f), 6.f);
+        const float s = mode == 1 ? 0.f : fminf(fmaxf(s_raw, -12.f), 6.f);
         const float er = y[2 * r] - mr, ei = y[2 * r + 1] - mi;
         const float iv = expf(-2.f * s);
         const float e2 = er * er + ei * ei;
         const float wr = w ? w[r] : 1.f;
         acc += wr * (0.5f * e2 * iv + 2.f * s);
         const float g = wr * inv_rows;
-        dout[3 * r] = -g * er * iv;
-        dout[3 * r + 1] = -g * ei * iv;
-        dout[3 * r + 2] = (s_raw > -12.f && s_raw < 6.f) ? g * (2.f - e2 * iv) : 0.f;
+        dout[3 * r] = mode == 2 ? 0.f : -g * er * iv;
+        dout[3 * r + 1] = mode == 2 ? 0.f : -g * ei * iv;
+        dout[3 * r + 2] = (mode != 1 && s_raw > -12.f && s_raw < 6.f) ? g * (2.f - e2 * iv) : 0.f;
     }
     red[threadIdx.x] = acc;
     __syncthreads();
@@ -222,10 +224,11 @@ int pnamp_mlp_linear_backward(const float *X, const float *W, const float *Y, fl
 
 int pnamp_mlp_loss_blocks(int rows) { return rows < 1 ? 1 : (grid_1d(rows) < 1024 ? grid_1d(rows) : 1024); }
 
-int pnamp_mlp_gauss_loss(const float *out, const float *y, const float *w, int rows, float *dout, float *loss_part,
-                         void *stream) {
-    if (!out || !y || !dout || !loss_part || rows < 1) return 1;
-    gauss_loss<<<pnamp_mlp_loss_blocks(rows), 256, 0, (cudaStream_t)stream>>>(out, y, w, rows, dout, loss_part);
+int pnamp_mlp_gauss_loss(const float *out, const float *y, const float *w, int rows, int mode, float *dout,
+                         float *loss_part, void *stream) {
+    if (!out || !y || !dout || !loss_part || rows < 1 || mode < 0 || mode > 2) return 1;
+    gauss_loss<<<pnamp_mlp_loss_blocks(rows), 256, 0, (cudaStream_t)stream>>>(out, y, w, rows, mode, dout,
+                                                                             loss_part);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 

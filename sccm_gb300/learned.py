@@ -223,7 +223,12 @@ class LearnedPNAMP:
         return torch.cat(xs), torch.cat(rs), torch.cat(ws)
 
     def fit(self, x_raw, resid, weight, epochs=None):
-        """Standardise the inputs, scale the targets, train with Adam; returns the loss history."""
+        """Standardise the inputs, scale the targets, train with Adam; returns the loss history.
+
+        The first three quarters of the epochs fit the mean by weighted least
+        squares, the rest fit the uncertainty to the mean's errors (mean left
+        alone): fitted jointly, the Gaussian likelihood lets the network widen
+        sigma where H/N is hard instead of fitting it."""
         cfg = self.cfg
         epochs = cfg.epochs if epochs is None else epochs
         self.mean = x_raw.mean(0).float().contiguous()
@@ -240,13 +245,16 @@ class LearnedPNAMP:
         gen = torch.Generator(device=self.dev)
         gen.manual_seed(cfg.seed)
         hist = []
+        e_mean = max(1, (3 * epochs) // 4)
         for ep in range(epochs):
             perm = torch.randperm(rows, device=self.dev, generator=gen)
-            lr = cfg.lr * (0.5 * (1 + math.cos(math.pi * ep / epochs)))       # cosine decay
+            mode, e0, ne = (1, 0, e_mean) if ep < e_mean else (2, e_mean, max(1, epochs - e_mean))
+            lr = cfg.lr * (0.5 * (1 + math.cos(math.pi * (ep - e0) / ne)))    # cosine decay per phase
             tot = torch.zeros((), device=self.dev)
             for b in range(nb):
                 idx = perm[b * bs:(b + 1) * bs]
-                tot += self.net.train_step(x[idx].contiguous(), y[idx].contiguous(), w[idx].contiguous(), lr=lr)
+                tot += self.net.train_step(x[idx].contiguous(), y[idx].contiguous(), w[idx].contiguous(), lr=lr,
+                                           mode=mode)
             hist.append(float(tot) / nb)
         self.history += hist
         return hist

@@ -33,7 +33,7 @@ def _lib():
         lib.pnamp_mlp_work_floats.restype = C.c_longlong
         lib.pnamp_mlp_linear_backward.argtypes = [vp, vp, vp, vp, vp, vp, vp, i, i, i, i, vp, vp]
         lib.pnamp_mlp_loss_blocks.argtypes = [i]
-        lib.pnamp_mlp_gauss_loss.argtypes = [vp, vp, vp, i, vp, vp, vp]
+        lib.pnamp_mlp_gauss_loss.argtypes = [vp, vp, vp, i, i, vp, vp, vp]
         lib.pnamp_mlp_adam.argtypes = [vp, vp, vp, vp, C.c_longlong, f, f, f, f, i, vp]
         lib.pnamp_learned_features.argtypes = [i, i, i, vp, C.c_longlong] + [vp] * 10
         lib.pnamp_learned_assemble.argtypes = [i, i, i, vp, vp, vp, C.c_double, vp, vp, vp, vp, vp]
@@ -134,13 +134,15 @@ class MLP:
                                               1 if k < L - 1 else 0, _p(self.work), C.c_void_p(st)),
                 "pnamp_mlp_linear_backward")
 
-    def loss_grad(self, out, y, w=None, stream=None):
-        """Gaussian loss of `out` [rows, 3] against y [rows, 2] (row weights w); returns (loss tensor, dout)."""
+    def loss_grad(self, out, y, w=None, mode=0, stream=None):
+        """Gaussian loss of `out` [rows, 3] against y [rows, 2] (row weights w); returns (loss tensor, dout).
+
+        mode 0: mean and uncertainty; 1: least squares on the mean; 2: the uncertainty only."""
         rows = out.shape[0]
         st = (stream or torch.cuda.current_stream()).cuda_stream
         dout = torch.empty_like(out)
         lp = self.loss_part
-        _ck(_lib().pnamp_mlp_gauss_loss(_p(out), _p(y), _p(w), rows, _p(dout), _p(lp), C.c_void_p(st)),
+        _ck(_lib().pnamp_mlp_gauss_loss(_p(out), _p(y), _p(w), rows, mode, _p(dout), _p(lp), C.c_void_p(st)),
             "pnamp_mlp_gauss_loss")
         return lp.sum(), dout
 
@@ -150,9 +152,9 @@ class MLP:
         _ck(_lib().pnamp_mlp_adam(_p(self.params), _p(self.grads), _p(self.m), _p(self.v), self.n_params,
                                   lr, beta1, beta2, eps, self.step, C.c_void_p(st)), "pnamp_mlp_adam")
 
-    def train_step(self, x, y, w=None, lr=1e-3):
+    def train_step(self, x, y, w=None, lr=1e-3, mode=0):
         out = self.forward(x)
-        loss, dout = self.loss_grad(out, y, w)
+        loss, dout = self.loss_grad(out, y, w, mode)
         self.backward(dout)
         self.adam(lr)
         return loss

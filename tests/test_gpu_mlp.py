@@ -52,6 +52,17 @@ def test_loss_and_gradients_match_oracle(setup):
             assert np.abs(g[lo:hi] - rg[lo:hi]).max() <= 1e-4 * sc, (k, lo)
 
 
+@pytest.mark.parametrize("mode", [1, 2])
+def test_loss_modes_match_oracle(setup, mode):
+    net, x, y, w = setup
+    dx, dy, dw = (torch.from_numpy(a).cuda() for a in (x, y, w))
+    out = net.forward(dx)
+    loss, dout = net.loss_grad(out, dy, dw, mode=mode)
+    rl, rdout = mo.gauss_loss(out.cpu().numpy().astype(np.float64), y, w, mode=mode)
+    assert abs(float(loss) - rl) <= 1e-5 * abs(rl)
+    assert np.abs(dout.cpu().numpy() - rdout).max() <= 1e-4 * np.abs(rdout).max()
+
+
 def test_adam_step_matches_oracle(setup):
     net, x, y, w = setup
     p0, g0 = net.state().astype(np.float64), net.grads.cpu().numpy().astype(np.float64)
