@@ -222,13 +222,14 @@ class LearnedPNAMP:
         self.mean, self.inv_std = mean, inv_std
         return torch.cat(xs), torch.cat(rs), torch.cat(ws)
 
-    def fit(self, x_raw, resid, weight, epochs=None):
+    def fit(self, x_raw, resid, weight, epochs=None, val_frac=0.1):
         """Standardise the inputs, scale the targets, train with Adam; returns the loss history.
 
-        The first three quarters of the epochs fit the mean by weighted least
-        squares, the rest fit the uncertainty to the mean's errors (mean left
-        alone): fitted jointly, the Gaussian likelihood lets the network widen
-        sigma where H/N is hard instead of fitting it."""
+        The mean and the uncertainty are fitted jointly (Gaussian likelihood,
+        |N|-weighted rows). A random `val_frac` of the rows is held out; the
+        parameters with the lowest held-out loss are kept (early stopping):
+        with the output layer starting at zero, the kept network is never
+        worse on held-out rows than the interpolation alone."""
         cfg = self.cfg
         epochs = cfg.epochs if epochs is None else epochs
         self.mean = x_raw.mean(0).float().contiguous()
@@ -239,23 +240,40 @@ class LearnedPNAMP:
         self.scale = float(torch.sqrt((wn * (resid ** 2).sum(1)).mean() / 2.0).clamp_min(1e-9))
         y = (resid / self.scale).float().contiguous()
         w = wn.float().contiguous()
-        rows = x.shape[0]
-        nb = max(1, rows // cfg.batch)
-        bs = rows // nb
         gen = torch.Generator(device=self.dev)
         gen.manual_seed(cfg.seed)
+        perm = torch.randperm(x.shape[0], device=self.dev, generator=gen)
+        nval = int(val_frac * x.shape[0])
+        vi, ti = perm[:nval], perm[nval:]
+        xv, yv, wv = x[vi].contiguous(), y[vi].contiguous(), w[vi].contiguous()
+        xt, yt, wt = x[ti].contiguous(), y[ti].contiguous(), w[ti].contiguous()
+        rows = xt.shape[0]
+        nb = max(1, rows // cfg.batch)
+        bs = rows // nb
+
+        def val_loss():
+            if nval == 0:
+                return 0.0
+            out = self.net.predict(xv)
+            s = out[:, 2].clamp(-12.0, 6.0)
+            e2 = ((yv - out[:, :2]) ** 2).sum(1)
+            return float((wv * (0.5 * e2 * torch.exp(-2.0 * s) + 2.0 * s)).mean())
+
+        best, best_params = val_loss(), self.net.params.clone()
         hist = []
-        e_mean = max(1, (3 * epochs) // 4)
         for ep in range(epochs):
-            perm = torch.randperm(rows, device=self.dev, generator=gen)
-            mode, e0, ne = (1, 0, e_mean) if ep < e_mean else (2, e_mean, max(1, epochs - e_mean))
-            lr = cfg.lr * (0.5 * (1 + math.cos(math.pi * (ep - e0) / ne)))    # cosine decay per phase
+            order = torch.randperm(rows, device=self.dev, generator=gen)
+            lr = cfg.lr * (0.5 * (1 + math.cos(math.pi * ep / epochs)))       # cosine decay
             tot = torch.zeros((), device=self.dev)
             for b in range(nb):
-                idx = perm[b * bs:(b + 1) * bs]
-                tot += self.net.train_step(x[idx].contiguous(), y[idx].contiguous(), w[idx].contiguous(), lr=lr,
-                                           mode=mode)
+                idx = order[b * bs:(b + 1) * bs]
+                tot += self.net.train_step(xt[idx].contiguous(), yt[idx].contiguous(), wt[idx].contiguous(), lr=lr)
             hist.append(float(tot) / nb)
+            v = val_loss()
+            if v < best:
+                best, best_params = v, self.net.params.clone()
+        self.net.params.copy_(best_params)
+        self.val_loss = best
         self.history += hist
         return hist
 

@@ -53,7 +53,7 @@ def _ck(rc, where):
 class MLP:
     """Parameters in one flat FP32 device buffer: per layer W [out][in] then b [out]."""
 
-    def __init__(self, n_in, width=256, depth=4, n_out=3, seed=0, device="cuda"):
+    def __init__(self, n_in, width=256, depth=4, n_out=3, seed=0, device="cuda", zero_output=True):
         self.dims = [n_in] + [width] * depth + [n_out]
         self.device = torch.device(device)
         sizes = [(self.dims[k + 1], self.dims[k]) for k in range(len(self.dims) - 1)]
@@ -65,10 +65,12 @@ class MLP:
         self.n_params = off
         rng = np.random.default_rng(seed)
         flat = np.zeros(off, dtype=np.float32)
-        for k, (o, i) in enumerate(sizes):
+        for k, (o, i) in enumerate(sizes[:-1] if zero_output else sizes):
             w0, b0 = self.offsets[k]
             lim = np.sqrt(6.0 / (i + o))                     # Glorot uniform
             flat[w0:b0] = rng.uniform(-lim, lim, o * i).astype(np.float32)
+        # zero_output: the output layer starts at zero, so an untrained network predicts 0
+        # (no correction to the interpolation, sigma = 1)
         self.params = torch.from_numpy(flat).to(self.device)
         self.grads = torch.zeros_like(self.params)
         self.m = torch.zeros_like(self.params)

@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 def setup():
     rng = np.random.default_rng(11)
     rows, n_in = 1000, 21                      # ragged against the 64-row tiles and 16-wide k steps
-    net = MLP(n_in, width=256, depth=4, seed=3)
+    net = MLP(n_in, width=256, depth=4, seed=3, zero_output=False)
     x = rng.normal(size=(rows, n_in)).astype(np.float32)
     y = rng.normal(size=(rows, 2)).astype(np.float32)
     w = rng.uniform(0.2, 2.0, rows).astype(np.float32)
@@ -77,7 +77,7 @@ def test_training_fits_a_smooth_function():
     rng = np.random.default_rng(2)
     x = rng.uniform(-1, 1, size=(8192, 4)).astype(np.float32)
     y = np.stack([np.sin(2 * x[:, 0]) * x[:, 1], np.cos(x[:, 2] + x[:, 3])], 1).astype(np.float32)
-    net = MLP(4, width=64, depth=2, seed=1)
+    net = MLP(4, width=64, depth=2, seed=1, zero_output=False)
     dx, dy = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
     first = float(net.train_step(dx, dy, lr=3e-3))
     for _ in range(800):
