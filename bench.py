@@ -154,6 +154,56 @@ UNEVEN_WORKLOAD = ("uneven batch: 64 sd pairs (n=24, Euler 8x16x8, gauge 7x7), 1
                    "10x20x10, 9x9), 16 sd+pf pairs (n=64, 12x24x12, 11x11)")
 
 
+def learned_main(args):
+    """`--workload learned`: learned + mixed against the exact mixed form on a fine-mesh pf set.
+
+    pf shell, `--learned-vacua` seeded deformed vacua (all symmetric pairs),
+    fine mesh 16 x 32 x 16 Euler x 11 x 11 gauge (991,232 points per pair),
+    coarse 4 x 8 x 4; the network (4 x 256) is trained on the first
+    `--learned-train` pairs. Reports both throughputs in fine-mesh points/s,
+    the fraction of Euler points computed exactly, and the errors of the
+    learned kernels against the exact ones (energy kernel in the basis of
+    normalised states, per-vacuum E_J, GCM levels).
+    """
+    import torch
+    from sccm_gb300.basis import Mesh
+    from sccm_gb300.learned import LearnedConfig, LearnedPNAMP, energy_errors_kev
+    from sccm_gb300.synth import make_workload
+
+    torch.cuda.set_device(0)
+    wl = make_workload("pf", args.learned_vacua, Mesh(16, 32, 16, 11), seed=4000)
+    lm = LearnedPNAMP(wl, LearnedConfig(train_euler=256, epochs=30, seed=3))
+    rec = lm.train(wl.pairs[:args.learned_train])
+    pts = len(wl.pairs) * lm.P * lm.G
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    exact, te = timed(lambda: lm.exact(wl.pairs))
+    learned, tl = timed(lambda: lm.run(wl.pairs))
+    base, tb = timed(lambda: lm.run(wl.pairs, use_net=False))
+    err = energy_errors_kev(learned, exact, nvac=len(wl.vacua), pairs=wl.pairs)
+    frac = sum(r["exact_euler"] for r in learned) / (len(learned) * lm.P)
+    print(json.dumps({
+        "metric": "projected kernel points/s, learned + mixed vs exact mixed (fine mesh)", "value": pts / tl,
+        "unit": "points/s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * tl, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "df64+f32", "data": "synthetic: seeded vacua and TBMEs",
+        "config": {"workload": f"pf n=40, {len(wl.vacua)} vacua ({len(wl.pairs)} pairs), Euler 16x32x16 x gauge "
+                               f"11x11, coarse 4x8x4, network 4x256 trained on {args.learned_train} pairs"},
+        "exact_mixed": {"value": pts / te, "seconds": te},
+        "without_network": {"value": pts / tb, "seconds": tb,
+                            "exact_fraction": sum(r["exact_euler"] for r in base) / (len(base) * lm.P)},
+        "exact_fraction": frac, "fallback_pairs": sum(r["fallback"] for r in learned),
+        "timing_s": lm.last_timing, "training": rec,
+        "errors_keV": {k: v for k, v in err.items() if k != "per_pair_keV"}}))
+    lm.close()
+    return 0
+
+
 def uneven_main(args):
     """`--workload uneven`: the three-model-space batch in persistent launches.
 
@@ -226,8 +276,11 @@ def main():
     ap.add_argument("--no-compare", action="store_true", help="skip timing the plain FP64 form as well")
     ap.add_argument("--mesh", default=None,
                     help="override the mesh as NALP,NBET,NGAM,NFOM (small cases for profiling captures)")
-    ap.add_argument("--workload", default="pf", choices=["pf", "uneven"],
-                    help="pf: the 210-pair pf-shell set (headline); uneven: three model spaces in one launch")
+    ap.add_argument("--workload", default="pf", choices=["pf", "uneven", "learned"],
+                    help="pf: the 210-pair pf-shell set (headline); uneven: three model spaces in one launch; "
+                         "learned: learned + mixed against exact mixed on a fine mesh")
+    ap.add_argument("--learned-vacua", type=int, default=6)
+    ap.add_argument("--learned-train", type=int, default=10)
     ap.add_argument("--uneven-scale", type=int, default=1, help="divide the uneven batch's pair counts")
     ap.add_argument("--tune-scale", type=int, default=16,
                     help="the autotuner times schedules on the uneven batch divided by this")
@@ -235,6 +288,8 @@ def main():
     args = ap.parse_args()
     if args.workload == "uneven":
         return uneven_main(args)
+    if args.workload == "learned":
+        return learned_main(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
