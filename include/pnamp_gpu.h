@@ -45,6 +45,8 @@ extern "C" {
 #define PNAMP_ERR_UNSUPPORTED 5  /* a size beyond what this build supports */
 #define PNAMP_ERR_STATE 6        /* call order violated */
 #define PNAMP_ERR_SCRATCH_LIMIT 7 /* request does not fit the fixed scratch of pnamp_batch_device_noalloc */
+#define PNAMP_ERR_SMALL_NORM 8   /* |N^0| <= CHOP: Write_ME1B prints a warning and writes nothing
+                                    (PNAMP_Rho1B.f90:74-77) */
 
 /* Size of the fixed device scratch array used by pnamp_batch_device_noalloc. */
 #define PNAMP_NOALLOC_SCRATCH_BYTES (32u << 20)
@@ -159,6 +161,33 @@ int pnamp_batch_device(pnamp_ctx *ctx, int npairs, const double *d_uv,
 int pnamp_batch_items_device(pnamp_ctx *ctx, int npairs, const double *d_uv,
                              long long nitems, const int *d_items, double *d_zres,
                              int *d_point_status, double *d_gauge_out, void *stream);
+
+/* ---- One-body density of the projected ground state (Rho1B) --------------
+ * Replaces ZRho1B_Angles / ZRho1B_Integral / Write_ME1B (PNAMP_Rho1B.f90:2-91,
+ * called from PNAMP_Kernel3D.f90:367,377,719): the J = 0 projected one-body
+ * density <q| rho_{(t lj n1), (t lj n2)} P^{J=0} P^N P^Z |q'> / <q| P |q'>,
+ * summed over m and divided by (2j + 1), per block (it, lj, n1, n2): it = 1
+ * protons, 0 neutrons; lj = l + j - 1/2; n1, n2 radial quantum numbers from 0.
+ *
+ * pnamp_rho1b_blocks returns the number of blocks and fills the arrays (each
+ * may be NULL) in Write_ME1B's order; a negative value is an error code. */
+int pnamp_rho1b_blocks(const pnamp_ctx *ctx, int *it, int *lj, int *n1, int *n2, int *twoj);
+
+/* pnamp_batch_device that also writes, per pair, block and Euler point, the
+ * gauge mean of N(Omega, phi) x sum_m rho / sqrt(2j + 1) (ZOBDJ0) into
+ * d_rho1b [npairs][nblocks][P_E] complex. PNAMP_ERR_STATE in norm-only mode. */
+int pnamp_batch_rho1b_device(pnamp_ctx *ctx, int npairs, const double *d_uv, double *d_zres,
+                             int *d_point_status, double *d_rho1b, void *stream);
+
+/* The same with host buffers (uv, zres, point_status as pnamp_batch; rho1b
+ * [npairs][nblocks][P_E] complex). */
+int pnamp_batch_rho1b(pnamp_ctx *ctx, int npairs, const double *uv, double *zres,
+                      int *point_status, double *rho1b);
+
+/* One pair's Write_ME1B values out[nblocks] = Re(sum_e w_e rho1b(e) / sum_e
+ * w_e N(e)) / sqrt(2j + 1) from its zres (ZRES(P_E, NOBS) column-major) and
+ * rho1b ([nblocks][P_E] complex). PNAMP_ERR_SMALL_NORM when |N^0| <= 1e-8. */
+int pnamp_project_rho1b(const pnamp_ctx *ctx, const double *zres, const double *rho1b, double *out);
 
 /* Same computation as pnamp_batch_device, for callers that must not allocate
  * device memory per call: code running under a runtime that owns the device

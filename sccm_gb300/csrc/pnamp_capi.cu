@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <vector>
 
@@ -40,6 +41,11 @@ struct pnamp_ctx {
     long long batch_cap = 0;
     cudaStream_t stream = nullptr;
     int sticky = 0;
+    // one-body density blocks (host copies) and the Euler quadrature weights
+    std::vector<int> r1b_it, r1b_lj, r1b_n1, r1b_n2, r1b_twoj;
+    std::vector<double> euler_w;
+    double *d_r1b = nullptr;
+    long long r1b_cap = 0;
 };
 
 namespace {
@@ -126,7 +132,7 @@ int plan_placement(Params &p, int smem_max) {
     pl.off_inv = fixed; fixed += align(n * 16);
     pl.off_red = fixed; fixed += align(40 * (kThreads / 32) * 8);  // 36 observable slots per warp
     pl.off_rot = fixed; fixed += align(p.rot_elems * 16);
-    pl.off_vec = fixed; fixed += align((N + kNobs + 2 * p.nfom) * 16);  // + phase tables
+    pl.off_vec = fixed; fixed += align((N + kNobs + 2 * p.nfom + p.obs.n_r1b) * 16);  // + phase tables
     // the Pfaffian matrix (N^2) shares storage with rho, kappa10, kappa01, K (4 n (n+1))
     const long long s_elems = std::max<long long>((long long)N * N, 4LL * n * (n + 1));
     const int bs = (int)(s_elems * 16), bt = (int)(nn * 16), by = (int)(2 * nn * 16), buv = (int)(2 * nn * 8);
@@ -202,6 +208,7 @@ const char *pnamp_strerror(int code) {
         case PNAMP_ERR_STATE: return "call order violated";
         case PNAMP_ERR_SCRATCH_LIMIT:
             return "request exceeds the fixed no-allocation scratch (PNAMP_NOALLOC_SCRATCH_BYTES)";
+        case PNAMP_ERR_SMALL_NORM: return "projected norm too small (|N^0| <= 1e-8) to normalise the density";
         default: return "unknown error";
     }
 }
@@ -225,6 +232,7 @@ int pnamp_set_outputs(pnamp_ctx *ctx, int outputs) {
 void pnamp_free(pnamp_ctx *ctx) {
     if (!ctx) return;
     for (void *q : ctx->allocs) cudaFree(q);
+    if (ctx->d_r1b) cudaFree(ctx->d_r1b);
     for (void *q : {(void *)ctx->d_pairbuf, (void *)ctx->d_scratch, (void *)ctx->d_uv, (void *)ctx->d_zres,
                     (void *)ctx->d_status, (void *)ctx->d_proj, (void *)ctx->d_projq})
         if (q) cudaFree(q);
@@ -395,6 +403,41 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
     UP(jp_d, ot.jp_d);
     UP(jm_d, ot.jm_d);
     UP(mz_d, ot.mz_d);
+    {   // one-body density blocks of ZRho1B_Angles (PNAMP_Rho1B.f90:14-29): states k1, k2 of the
+        // same isospin, lj and m; it = 1 for protons (t = -1), 0 for neutrons; ordered it, lj, n1, n2
+        // as Write_ME1B loops (PNAMP_Rho1B.f90:80-88)
+        std::map<std::vector<int>, std::vector<int>> blocks;
+        for (int k1 = 0; k1 < n; ++k1)
+            for (int k2 = 0; k2 < n; ++k2) {
+                const int lj1 = (2 * sp->l[k1] + sp->twoj[k1] - 1) / 2, lj2 = (2 * sp->l[k2] + sp->twoj[k2] - 1) / 2;
+                if (sp->t[k1] != sp->t[k2] || lj1 != lj2 || sp->twom[k1] != sp->twom[k2]) continue;
+                const int it = sp->t[k1] == -1 ? 1 : 0;
+                blocks[{it, lj1, sp->n[k1] - 1, sp->n[k2] - 1, sp->twoj[k1]}].push_back(k1 * 256 + k2);
+            }
+        std::vector<int> off{0}, idx;
+        std::vector<double> val;
+        if ((int)blocks.size() <= kMaxR1B) {
+            for (const auto &kv : blocks) {
+                c->r1b_it.push_back(kv.first[0]);
+                c->r1b_lj.push_back(kv.first[1]);
+                c->r1b_n1.push_back(kv.first[2]);
+                c->r1b_n2.push_back(kv.first[3]);
+                c->r1b_twoj.push_back(kv.first[4]);
+                for (int e : kv.second) {
+                    idx.push_back(e);
+                    val.push_back(1.0 / std::sqrt(kv.first[4] + 1.0));
+                }
+                off.push_back((int)idx.size());
+            }
+        }
+        ot.n_r1b = (int)c->r1b_it.size();
+        UP(off, ot.r1b_off);
+        if (!idx.empty()) {
+            UP(idx, ot.r1b_idx);
+            UP(val, ot.r1b_val);
+        }
+        for (size_t e = 3; e < euler.size(); e += 4) c->euler_w.push_back(euler[e]);
+    }
 #undef UP
     p.obs = ot;
     int smem_optin = 0, nsm = 0;
@@ -484,6 +527,89 @@ int pnamp_batch_items_device(pnamp_ctx *c, int npairs, const double *d_uv, long 
     const int grid = (int)std::min<long long>(c->grid_form[c->p.form], nitems);
     CK(launch_points(c->p, npairs, c->d_pairbuf, c->d_scratch, grid, d_zres, d_status, st,
                      reinterpret_cast<const int2 *>(d_items), nitems, d_gauge_out));
+    return PNAMP_OK;
+}
+
+int pnamp_rho1b_blocks(const pnamp_ctx *c, int *it, int *lj, int *n1, int *n2, int *twoj) {
+    if (!c) return -PNAMP_ERR_ARG;
+    const int nb = (int)c->r1b_it.size();
+    for (int b = 0; b < nb; ++b) {
+        if (it) it[b] = c->r1b_it[b];
+        if (lj) lj[b] = c->r1b_lj[b];
+        if (n1) n1[b] = c->r1b_n1[b];
+        if (n2) n2[b] = c->r1b_n2[b];
+        if (twoj) twoj[b] = c->r1b_twoj[b];
+    }
+    return nb;
+}
+
+int pnamp_batch_rho1b_device(pnamp_ctx *c, int npairs, const double *d_uv, double *d_zres, int *d_status,
+                             double *d_rho1b, void *stream) {
+    if (!c || npairs < 0 || (npairs > 0 && (!d_uv || !d_zres || !d_status || !d_rho1b))) return PNAMP_ERR_ARG;
+    if (c->p.obs.n_r1b == 0) return PNAMP_ERR_UNSUPPORTED;
+    if (c->p.norm_only) return PNAMP_ERR_STATE;
+    if (npairs == 0) return PNAMP_OK;
+    int rc = ensure_pairs(c, npairs);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
+    CK(launch_setup(c->p, npairs, d_uv, c->d_pairbuf, st));
+    CK(launch_points(c->p, npairs, c->d_pairbuf, c->d_scratch, c->grid_form[c->p.form], d_zres, d_status, st,
+                     nullptr, 0, nullptr, d_rho1b));
+    return PNAMP_OK;
+}
+
+int pnamp_batch_rho1b(pnamp_ctx *c, int npairs, const double *uv, double *zres, int *point_status,
+                      double *rho1b) {
+    if (!c || npairs < 0 || (npairs > 0 && (!uv || !zres || !rho1b))) return PNAMP_ERR_ARG;
+    if (npairs == 0) return PNAMP_OK;
+    int rc = ensure_batch(c, npairs);
+    if (rc) return rc;
+    const long long rb = (long long)npairs * c->p.obs.n_r1b * c->p.n_euler * 2;
+    if (rb > c->r1b_cap) {
+        if (c->d_r1b) cudaFree(c->d_r1b);
+        c->d_r1b = nullptr;
+        c->r1b_cap = 0;
+        CK(cudaMalloc(&c->d_r1b, (size_t)rb * sizeof(double)));
+        c->r1b_cap = rb;
+    }
+    const long long nn = (long long)c->p.n * c->p.n;
+    const size_t zbytes = (size_t)npairs * 2 * kNobs * c->p.n_euler * sizeof(double);
+    const size_t sbytes = (size_t)npairs * c->p.n_euler * sizeof(int);
+    CK(cudaMemcpyAsync(c->d_uv, uv, (size_t)npairs * 4 * nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    rc = pnamp_batch_rho1b_device(c, npairs, c->d_uv, c->d_zres, c->d_status, c->d_r1b, c->stream);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(zres, c->d_zres, zbytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(rho1b, c->d_r1b, (size_t)rb * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    std::vector<int> st((size_t)npairs * c->p.n_euler);
+    CK(cudaMemcpyAsync(st.data(), c->d_status, sbytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (point_status) memcpy(point_status, st.data(), sbytes);
+    for (int v : st)
+        if (v & PNAMP_ST_SINGULAR_U) return PNAMP_ERR_SINGULAR_U;
+    return PNAMP_OK;
+}
+
+int pnamp_project_rho1b(const pnamp_ctx *c, const double *zres, const double *rho1b, double *out) {
+    if (!c || !zres || !rho1b || !out) return PNAMP_ERR_ARG;
+    const int P = c->p.n_euler, nb = (int)c->r1b_it.size();
+    // J = 0 projection (ZRho1B_Integral, PNAMP_Rho1B.f90:36-60) over the Euler weights; the J = 0
+    // weight and, for K = 0, the D-function are common to numerator and norm and cancel in the ratio
+    double nr = 0.0, ni = 0.0;
+    for (int e = 0; e < P; ++e) {
+        nr += c->euler_w[e] * zres[2 * e];
+        ni += c->euler_w[e] * zres[2 * e + 1];
+    }
+    if (std::sqrt(nr * nr + ni * ni) <= 1e-8) return PNAMP_ERR_SMALL_NORM;  // Write_ME1B: CHOP
+    const double d = nr * nr + ni * ni;
+    for (int b = 0; b < nb; ++b) {
+        double sr = 0.0, si = 0.0;
+        for (int e = 0; e < P; ++e) {
+            sr += c->euler_w[e] * rho1b[2 * ((long long)b * P + e)];
+            si += c->euler_w[e] * rho1b[2 * ((long long)b * P + e) + 1];
+        }
+        // AE = Re(sum / N), written divided by sqrt(2j + 1) (PNAMP_Rho1B.f90:82-84)
+        out[b] = (sr * nr + si * ni) / d / std::sqrt(c->r1b_twoj[b] + 1.0);
+    }
     return PNAMP_OK;
 }
 

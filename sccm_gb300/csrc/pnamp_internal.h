@@ -55,7 +55,13 @@ struct ObsTables {
     const double *mz;          // [n] m_a
     const double *jj1;         // [n] j(j+1)
     const dd *jp_d, *jm_d, *mz_d;   // the same coefficients as double-float
+    // one-body density blocks (t, lj, n1, n2) of ZRho1B_Angles: block b sums
+    // r1b_val[e] rho(row, col) over e in [r1b_off[b], r1b_off[b + 1]), packed row*256+col
+    int n_r1b;
+    const int *r1b_off, *r1b_idx;
+    const double *r1b_val;
 };
+constexpr int kMaxR1B = 64;               // one-body density blocks per model space
 
 struct Params {
     int n, h, N2;              // n, n/2, 2n
@@ -97,7 +103,8 @@ cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *
                          cudaStream_t st);
 cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc *scratch,
                           int grid, double *zres, int *status, cudaStream_t st,
-                          const int2 *items = nullptr, long long nitems = 0, double *gout = nullptr);
+                          const int2 *items = nullptr, long long nitems = 0, double *gout = nullptr,
+                          double *r1out = nullptr);
 cudaError_t launch_proj_weights(const Params &p, int axial, zc *w, cudaStream_t st);
 cudaError_t launch_project(const Params &p, int npairs, const zc *w, const double *zres,
                            int core_prot, int core_neut, int chop, double *out, cudaStream_t st);

@@ -401,6 +401,7 @@ cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *
 
 // ------------------------------------------------------------------ points
 constexpr int kNSlot = 36;  // observable sums: slots 0..37 final values, then per-warp partials
+constexpr int kR1BSlot = 128;  // one-body density block sums: red[kR1BSlot + 2b], re and im
 static_assert(kThreads >= 32 * (kNTrace + 1), "one warp per Q trace plus warp 0");
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -416,7 +417,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 template <class Z>
 __device__ __forceinline__ void point_item(const Params &p, const double *__restrict__ pairbuf, zc *slot,
                                            int pair, int ie, bool reload, double *__restrict__ zres,
-                                           int *__restrict__ status, double *__restrict__ gout = nullptr) {
+                                           int *__restrict__ status, double *__restrict__ gout = nullptr,
+                                           double *__restrict__ r1out = nullptr) {
     using A = Ar<Z>;
     using R = typename A::R;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -445,6 +447,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
     zc *acc = reinterpret_cast<zc *>(vec + N);      // kNobs accumulators (thread 0)
     zc *eph = acc + kNobs;                          // e^{i phi_l}, l < NFOM
     Z *ephz = reinterpret_cast<Z *>(eph + p.nfom);  // the same in the point arithmetic
+    zc *acc_r1b = reinterpret_cast<zc *>(ephz + p.nfom);  // one-body density blocks (thread 0)
     Z *rho = S, *k10 = S + n * ld, *k01 = S + 2 * n * ld;
     Z *Kc = S + 3 * n * ld;  // antisymmetrised pairing tensors
 
@@ -492,6 +495,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
         }
         if (threadIdx.x == 0) {
             for (int io = 0; io < kNobs; ++io) acc[io] = mk(0.0, 0.0);
+            for (int b = 0; b < (r1out ? p.obs.n_r1b : 0); ++b) acc_r1b[b] = mk(0.0, 0.0);
         }
         __syncthreads();
         // ---- R W (or, for the Onishi norm, R U1 and conj(R) V1), R V1, conj(R) U1 (FP64)
@@ -701,6 +705,23 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         fin[19 + 2 * q] = si;
                     }
                 }
+                if (r1out && wid > kNTrace) {  // one-body density blocks (ZRho1B_Angles): the idle warps
+                    for (int b = wid - kNTrace - 1; b < p.obs.n_r1b; b += nw - kNTrace - 1) {
+                        double sr = 0.0, si = 0.0;
+                        for (int e = p.obs.r1b_off[b] + lane; e < p.obs.r1b_off[b + 1]; e += 32) {
+                            const int ix = p.obs.r1b_idx[e];
+                            const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
+                            sr = fma(p.obs.r1b_val[e], r.x, sr);
+                            si = fma(p.obs.r1b_val[e], r.y, si);
+                        }
+                        sr = warp_sum(sr);
+                        si = warp_sum(si);
+                        if (lane == 0) {
+                            red[kR1BSlot + 2 * b] = sr;
+                            red[kR1BSlot + 2 * b + 1] = si;
+                        }
+                    }
+                }
                 auto put = [&](int slot, double v) {  // slot 0..3: energy re/im, <J^2> re/im
                     v = warp_sum(v);
                     if (lane == 0) pw[slot * nw + wid] = v;
@@ -806,6 +827,8 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         acc[3] = zfma(norm, ekin, acc[3]);
                         acc[6] = zfma(norm, hg, acc[6]);
                         acc[7] = zfma(norm, j2, acc[7]);
+                        for (int b = 0; b < (r1out ? p.obs.n_r1b : 0); ++b)
+                            acc_r1b[b] = zfma(norm, mk(red[kR1BSlot + 2 * b], red[kR1BSlot + 2 * b + 1]), acc_r1b[b]);
                         if (p.iE2)
                             for (int q = 0; q < 5; ++q) {
                                 acc[8 + q] = zfma(norm, mk(get(18 + 2 * q), get(19 + 2 * q)), acc[8 + q]);
@@ -828,6 +851,11 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 zout[2LL * (io * p.n_euler + ie) + 1] = v.y;
             }
             status[(long long)pair * p.n_euler + ie] = f;
+            for (int b = 0; b < (r1out ? p.obs.n_r1b : 0); ++b) {
+                const zc v = inv * acc_r1b[b];
+                r1out[2LL * (((long long)pair * p.obs.n_r1b + b) * p.n_euler + ie)] = v.x;
+                r1out[2LL * (((long long)pair * p.obs.n_r1b + b) * p.n_euler + ie) + 1] = v.y;
+            }
         }
         __syncthreads();
     }
@@ -837,7 +865,7 @@ template <class Z>
 __global__ void __launch_bounds__(kThreads, 1)
 point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scratch,
              double *__restrict__ zres, int *__restrict__ status, const int2 *__restrict__ items,
-             long long nitems, double *__restrict__ gout) {
+             long long nitems, double *__restrict__ gout, double *__restrict__ r1out) {
     // items == nullptr: every (pair, Euler point) of the batch; else the listed (pair, ie)
     zc *slot = scratch + (long long)blockIdx.x * p.place.slot_elems;
     const long long total = items ? nitems : (long long)npairs * p.n_euler;
@@ -853,7 +881,7 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
             pair = (int)(item / p.n_euler);
             ie = (int)(item % p.n_euler);
         }
-        point_item<Z>(p, pairbuf, slot, pair, ie, pair != cur_pair, zres, status, gout);
+        point_item<Z>(p, pairbuf, slot, pair, ie, pair != cur_pair, zres, status, gout, r1out);
         cur_pair = pair;
     }
 }
@@ -945,13 +973,13 @@ cudaError_t set_point_smem(int form, int bytes) {
 
 cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc *scratch, int grid,
                           double *zres, int *status, cudaStream_t st, const int2 *items, long long nitems,
-                          double *gout) {
+                          double *gout, double *r1out) {
     if (p.form == 1)
         point_kernel<zd><<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status,
-                                                                    items, nitems, gout);
+                                                                    items, nitems, gout, r1out);
     else
         point_kernel<zc><<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status,
-                                                                    items, nitems, gout);
+                                                                    items, nitems, gout, r1out);
     return cudaGetLastError();
 }
 

@@ -45,9 +45,11 @@ EXPORTS = ("pnamp_init", "pnamp_n_euler", "pnamp_pair", "pnamp_batch", "pnamp_ba
            "pnamp_strerror", "pnamp_version", "pnamp_batch_device_noalloc", "pnamp_set_form",
            "pnamp_project_q", "pnamp_project_q_device", "pnamp_multi_create", "pnamp_multi_schedule",
            "pnamp_multi_launch", "pnamp_multi_items", "pnamp_multi_free", "pnamp_multi_placement",
-           "pnamp_set_outputs", "pnamp_batch_items_device")
+           "pnamp_set_outputs", "pnamp_batch_items_device", "pnamp_rho1b_blocks", "pnamp_batch_rho1b_device",
+           "pnamp_batch_rho1b", "pnamp_project_rho1b")
 FORMS = {"fp64": 0, "df64": 1}
 PNAMP_ERR_SCRATCH_LIMIT = 7
+PNAMP_ERR_SMALL_NORM = 8
 
 
 class PnampError(RuntimeError):
@@ -98,6 +100,11 @@ def load_library(path: str | None = None):
     lib.pnamp_n_euler.argtypes = [vp]
     lib.pnamp_set_form.argtypes = [vp, C.c_int]
     lib.pnamp_set_outputs.argtypes = [vp, C.c_int]
+    lib.pnamp_rho1b_blocks.argtypes = [vp] + [C.POINTER(C.c_int)] * 5
+    lib.pnamp_batch_rho1b_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp]
+    lib.pnamp_batch_rho1b.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    lib.pnamp_project_rho1b.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.pnamp_batch_items_device.argtypes = [vp, C.c_int, vp, C.c_longlong, vp, vp, vp, vp, vp]
     lib.pnamp_pair.argtypes = [vp] + [C.POINTER(C.c_double)] * 5 + [C.POINTER(C.c_int)]
     lib.pnamp_batch.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -280,6 +287,42 @@ class PnampContext:
         if rc != PNAMP_OK:
             raise PnampError(rc, "pnamp_project_q")
         return qp, qc
+
+    def rho1b_blocks(self):
+        """[(it, lj, n1, n2, twoj)] of the one-body density, in Write_ME1B's order."""
+        lib = load_library()
+        nb = lib.pnamp_rho1b_blocks(self._h, None, None, None, None, None)
+        if nb < 0:
+            raise PnampError(-nb, "pnamp_rho1b_blocks")
+        arrs = [np.zeros(nb, dtype=np.int32) for _ in range(5)]
+        lib.pnamp_rho1b_blocks(self._h, *[_iptr(a) for a in arrs])
+        return [tuple(int(a[b]) for a in arrs) for b in range(nb)]
+
+    def batch_rho1b(self, pairs_or_packed):
+        """-> (zres [npairs, P_E, NOBS], status, rho1b [npairs, nblocks, P_E]) through the host-buffer ABI."""
+        uv = pairs_or_packed if isinstance(pairs_or_packed, np.ndarray) else self.pack_pairs(pairs_or_packed)
+        uv = np.ascontiguousarray(uv, dtype=np.float64)
+        npairs = uv.shape[0]
+        nb = len(self.rho1b_blocks())
+        z = np.zeros((npairs, NOBS, self.n_euler), dtype=np.complex128)
+        st = np.zeros((npairs, self.n_euler), dtype=np.int32)
+        r = np.zeros((npairs, nb, self.n_euler), dtype=np.complex128)
+        rc = load_library().pnamp_batch_rho1b(self._h, npairs, _dptr(uv), z.ctypes.data_as(C.POINTER(C.c_double)),
+                                              _iptr(st), r.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_batch_rho1b")
+        return np.ascontiguousarray(z.transpose(0, 2, 1)), st, r
+
+    def project_rho1b(self, zres, rho1b):
+        """One pair: zres [P_E, NOBS], rho1b [nblocks, P_E] -> Write_ME1B values [nblocks]."""
+        z = np.ascontiguousarray(np.asarray(zres, dtype=np.complex128).T)
+        r = np.ascontiguousarray(np.asarray(rho1b, dtype=np.complex128))
+        out = np.zeros(r.shape[0])
+        rc = load_library().pnamp_project_rho1b(self._h, z.ctypes.data_as(C.POINTER(C.c_double)),
+                                                r.ctypes.data_as(C.POINTER(C.c_double)), _dptr(out))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_project_rho1b")
+        return out
 
     def set_outputs(self, outputs):
         """"all" (19 observables) or "norm" (N(Omega) only) for later batches."""
