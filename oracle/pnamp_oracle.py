@@ -25,6 +25,7 @@ Reference files (paths inside jmyao17/SCCM):
   PNAMP_ME1B.f90       ZN_0, ZQ2, ZQ2t
   PNAMP_ME2B.f90       ZJ2_0
   PNAMP_Onishi.f90     Onishi
+  PNAMP_Rho1B.f90      ZRho1B_Angles, ZRho1B_Integral, Write_ME1B
 """
 from __future__ import annotations
 
@@ -253,13 +254,55 @@ def point_observables(sp, ham, A, U0, V0, U1, V1, znorm, iE2=True):
     return out
 
 
+def rho1b_table(sp: ModelSpace):
+    """Blocks of ZRho1B_Angles (PNAMP_Rho1B.f90:14-29): [(it, lj, n1, n2, twoj), [(k1, k2), ...]].
+
+    States k1, k2 of the same isospin, lj and m; it = 1 for protons (t = -1), 0
+    for neutrons; n from 0; ordered it, lj, n1, n2 as Write_ME1B loops
+    (PNAMP_Rho1B.f90:80-88)."""
+    blocks = {}
+    n = sp.nlev
+    for k1 in range(n):
+        for k2 in range(n):
+            if sp.t[k1] != sp.t[k2] or sp.lj[k1] != sp.lj[k2] or sp.twom[k1] != sp.twom[k2]:
+                continue
+            it = 1 if sp.t[k1] == -1 else 0
+            key = (it, int(sp.lj[k1]), int(sp.n[k1]) - 1, int(sp.n[k2]) - 1, int(sp.twoj[k1]))
+            blocks.setdefault(key, []).append((k1, k2))
+    return sorted(blocks.items())
+
+
+def rho1b_point(table, rho, znorm):
+    """ZRho1B_Angles for one gauge point: znorm * sum ZRO(k1, k2) / sqrt(2j + 1) per block
+    (the 1/NFOM^2 is applied with the gauge mean)."""
+    return np.array([znorm * sum(rho[k1, k2] for k1, k2 in ent) / math.sqrt(key[4] + 1.0)
+                     for key, ent in table], complex)
+
+
+def rho1b_write_me1b(table, zres, r, mesh: Mesh):
+    """ZRho1B_Integral at J = 0 and Write_ME1B (PNAMP_Rho1B.f90:36-91) for one pair.
+
+    r [P_E, nblocks] are the gauge means from `kernel_triaxial(..., rho1b=...)`.
+    Returns Re(sum_e w_e r_e / N^0) / sqrt(2j + 1) per block (the J = 0 weight
+    cancels in the ratio), or None when |N^0| <= CHOP (the reference warns and
+    writes nothing)."""
+    w = mesh.euler_points()[:, 3]
+    zn = np.sum(w * zres[:, 0])
+    if abs(zn) <= CHOP:
+        return None
+    zr = w @ r
+    return np.array([np.real(zr[b] / zn) / math.sqrt(key[4] + 1.0) for b, (key, _) in enumerate(table)])
+
+
 def kernel_triaxial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1,
-                    cscale=1.0, iscale=0, iE2=True, euler_subset=None, point_log=None):
+                    cscale=1.0, iscale=0, iE2=True, euler_subset=None, point_log=None, rho1b=None):
     """Kernel4Triaxial mesh loop (PNAMP_Kernel3D.f90:70-407) -> ZRES[P_E, NOBS].
 
     Shell-model runs take the Pfaffian branch (ide forced to 1, Kernel3D.f90:140-159)
     unless NFOM = 1, where the Onishi formula gives the norm (Kernel3D.f90:286-290). `euler_subset` restricts the loop to a list of Euler
     indices (rows of ZRES left zero elsewhere) so tests can sample large meshes.
+    With `rho1b` (a `rho1b_table`), returns (ZRES, R) with R[P_E, nblocks] the
+    gauge means of ZRho1B_Angles (Kernel3D.f90:367).
     """
     n = sp.nlev
     U0, V0, U1, V1 = (np.asarray(x, dtype=float) for x in (U0, V0, U1, V1))
@@ -273,6 +316,7 @@ def kernel_triaxial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1
     phis = mesh.gauge_angles()
     nf = mesh.nfom
     zres = np.zeros((len(pts), NOBS), complex)
+    r1 = np.zeros((len(pts), len(rho1b) if rho1b is not None else 0), complex)
     idx = range(len(pts)) if euler_subset is None else euler_subset
     for ie in idx:
         alp, bet, gam, _w = pts[ie]
@@ -293,8 +337,11 @@ def kernel_triaxial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1
                 if point_log is not None:
                     point_log.append((ie, php, phn, pf, o))
                 acc += o
+                if rho1b is not None:
+                    r1[ie] += rho1b_point(rho1b, rokappa(A, U0, V0, U1, V1)[0], znorm)
         zres[ie] = acc / nf ** 2
-    return zres
+        r1[ie] /= nf ** 2
+    return (zres, r1) if rho1b is not None else zres
 
 
 def kernel_axial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1, iE2=True):

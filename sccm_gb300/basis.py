@@ -38,6 +38,8 @@ SHELLS = {
     "pf": [(0, 3, 7), (1, 1, 3), (0, 3, 5), (1, 1, 1)],
     "pf5g9": [(0, 3, 5), (1, 1, 3), (1, 1, 1), (0, 4, 9)],
     "sdpf": [(0, 2, 5), (1, 0, 1), (0, 2, 3), (0, 3, 7), (1, 1, 3), (0, 3, 5), (1, 1, 1)],
+    # two p1/2 orbits: one-body density blocks with n1 != n2 (test space)
+    "p2": [(0, 1, 3), (0, 1, 1), (1, 1, 1)],
 }
 
 

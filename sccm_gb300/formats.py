@@ -20,12 +20,13 @@ consume this implementation's files unchanged:
 """
 from __future__ import annotations
 
+import math
 import os
 import struct
 
 import numpy as np
 
-from .basis import JJMAX, ModelSpace
+from .basis import CHOP, JJMAX, ModelSpace
 
 
 class FormatError(ValueError):
@@ -356,3 +357,24 @@ def atomic_write_text(path, writer, *args, **kw):
     tmp = f"{path}.tmp{os.getpid()}"
     writer(tmp, *args, **kw)
     os.replace(tmp, path)
+
+
+# ---------------------------------------------------------------- Rho1B density files
+def write_rho1b_dens(path, blocks, values, chop=CHOP):
+    """Write_ME1B (PNAMP_Rho1B.f90:63-91): one line '(4i5,f20.10)' it, lj, n1, n2, value per
+    block whose AE = value * sqrt(2j + 1) exceeds CHOP. `blocks` are (it, lj, n1, n2, twoj)."""
+    with open(path, "w") as f:
+        for (it, lj, n1, n2, twoj), v in zip(blocks, values):
+            if abs(v * math.sqrt(twoj + 1.0)) > chop:
+                f.write(f"{it:5d}{lj:5d}{n1:5d}{n2:5d}{v:20.10f}\n")
+
+
+def read_rho1b_dens(path):
+    """A Write_ME1B file -> {(it, lj, n1, n2): value}."""
+    out = {}
+    with open(path) as f:
+        for ln in f:
+            tok = ln.split()
+            if len(tok) == 5:
+                out[tuple(int(x) for x in tok[:4])] = float(tok[4])
+    return out

@@ -28,4 +28,5 @@ def ge76():
     return dict(sp=sp, e0=float(d["e0"]), t1b=onebody_matrix(sp, spe), recs=recs, vbar=d["vbar"],
                 U=d["U"], V=d["V"], gold=d["gold"], betas=d["betas"], jvals=d["jvals"],
                 nfom=int(d["nfom"]), nbet=int(d["nbet"]), ncosbet=int(d["ncosbet"]),
-                q2=q2_operators(sp), jops=j_operators(sp))
+                q2=q2_operators(sp), jops=j_operators(sp),
+                rho1b_keys=[tuple(int(x) for x in k) for k in d["rho1b_keys"]], rho1b_gold=d["rho1b_gold"])

@@ -12,7 +12,10 @@ need, so the tests never read the reference tree at run time:
     (data/Ge/Ge76_HFB_GCN2850_pf5g9_hwHO09_s000_beta*gam00np00cf000.wf)
   * the reference's kernel files for the 16 pairs among those four vacua
     (data/Ge/kern.1D.05.01.16.01.GCN2850_pf5g9_hwHO09_s000_*.elem):
-    N^J, H^J, <N>, <Z>, <J^2> at J = 0, 2, 4, 6.
+    N^J, H^J, <N>, <Z>, <J^2> at J = 0, 2, 4, 6;
+  * the reference's J = 0 one-body density files of the same pairs
+    (data/Ge/Rho1B.Ge76.1D.05.01.16.01.pf5g9_hwHO09_s000_*.dens): per block
+    (it, lj, n1, n2) the value Write_ME1B prints.
 
 The beta2 = -0.2 vacuum is left out: no beta sign, pair order or quadrature
 reproduces the shipped kernel files of its 9 pairs (errors 1e-4 to 1e-1 where
@@ -32,7 +35,7 @@ sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
 
 from sccm_gb300.basis import ModelSpace  # noqa: E402
 from sccm_gb300.formats import (mscheme_pairs, read_elem_axial, read_me1b,  # noqa: E402
-                                read_mscheme_binary, read_val, read_wf)
+                                read_mscheme_binary, read_rho1b_dens, read_val, read_wf)
 
 REF = os.environ.get("SCCM_REF", "/root/reference")
 BETAS = (-10, 0, 10, 20)       # beta2 x 100
@@ -47,6 +50,12 @@ def elem_name(b1, b2):
     f = lambda b: f"+{b * 100:05d}" if b >= 0 else f"-{-b * 100:05d}"
     return (f"{REF}/data/Ge/kern.1D.05.01.16.01.GCN2850_pf5g9_hwHO09_s000_"
             f"{f(b1)}.000cf000_{f(b2)}.000cf000.elem")
+
+
+def rho1b_name(b1, b2):
+    f = lambda b: f"+{b * 100:05d}" if b >= 0 else f"-{-b * 100:05d}"
+    return (f"{REF}/data/Ge/Rho1B.Ge76.1D.05.01.16.01.pf5g9_hwHO09_s000_"
+            f"{f(b1)}.000cf000_{f(b2)}.000cf000.dens")
 
 
 def main(out=os.path.join(HERE, "ge76_fixture.npz")):
@@ -68,13 +77,22 @@ def main(out=os.path.join(HERE, "ge76_fixture.npz")):
             for jj, J in enumerate((0, 2, 4, 6)):
                 for f, name in enumerate(fields):
                     gold[i, j, jj, f] = g[J][name]
+    dens = {(i, j): read_rho1b_dens(rho1b_name(b1, b2))
+            for i, b1 in enumerate(BETAS) for j, b2 in enumerate(BETAS)}
+    rho1b_keys = sorted({k for d in dens.values() for k in d})
+    rho1b_gold = np.full((len(BETAS), len(BETAS), len(rho1b_keys)), np.nan)
+    for (i, j), d in dens.items():
+        for b, k in enumerate(rho1b_keys):
+            if k in d:
+                rho1b_gold[i, j, b] = d[k]
     spe_keys = np.array(sorted(spe), dtype=np.int32)
     spe_vals = np.array([spe[tuple(k)] for k in spe_keys])
     np.savez_compressed(out, orbits=np.array(orbits, dtype=np.int32), e0=e0,
                         spe_keys=spe_keys, spe_vals=spe_vals, vbar=vbar,
                         betas=np.array(BETAS) / 100.0, U=U, V=V, gold=gold,
                         fields=np.array(fields), jvals=np.array([0, 2, 4, 6]),
-                        nprot=4, nneut=16, core=28, nfom=5, nbet=16, ncosbet=2)
+                        nprot=4, nneut=16, core=28, nfom=5, nbet=16, ncosbet=2,
+                        rho1b_keys=np.array(rho1b_keys, dtype=np.int32), rho1b_gold=rho1b_gold)
     print(f"wrote {out}: {os.path.getsize(out)} bytes")
 
 

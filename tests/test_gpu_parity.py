@@ -218,3 +218,37 @@ def test_driver_writes_kernel_files_and_resumes(sd, tmp_path):
     for f in ("njkk", "hjkk"):
         sc = np.abs(kern[f]).max()
         assert np.abs(r[f][::2] - kern[f][::2]).max() <= 1e-7 * sc
+
+
+RHO1B_TOL = 2e-9   # the reference's .dens files print 10 decimals
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_ge76_rho1b_files_through_gpu(ge76, form):
+    """The J = 0 one-body densities of the 16 Ge76 pairs reproduce data/Ge/Rho1B.*.dens."""
+    g = ge76
+    mesh = Mesh(1, g["nbet"], 1, g["nfom"], ncosbet=g["ncosbet"])
+    idx = [(i, j) for i in range(4) for j in range(4)]
+    with PnampContext(g["sp"], g["e0"], g["t1b"], g["recs"], g["vbar"], mesh, q2=None, form=form) as ctx:
+        assert [b[:4] for b in ctx.rho1b_blocks()] == g["rho1b_keys"]
+        z, _, r = ctx.batch_rho1b([(g["U"][i], g["V"][i], g["U"][j], g["V"][j]) for i, j in idx])
+        for k, (i, j) in enumerate(idx):
+            vals = ctx.project_rho1b(z[k], r[k])
+            assert np.abs(vals - g["rho1b_gold"][i, j]).max() <= RHO1B_TOL, ((i, j), vals)
+
+
+def test_rho1b_blocks_with_two_radial_orbits_match_oracle():
+    """A space with 0p1/2 and 1p1/2: off-diagonal (n1 != n2) blocks against the oracle."""
+    from oracle.pnamp_oracle import rho1b_table
+    w = make_workload("p2", 3, Mesh(2, 3, 2, 3), seed=909)
+    ham = Hamiltonian(w.e0, w.t1b, w.recs, w.vbar, w.q2, w.jops)
+    table = rho1b_table(w.sp)
+    assert any(k[2] != k[3] for k, _ in table)
+    with ctx_for(w, w.mesh) as ctx:
+        assert ctx.rho1b_blocks() == [k for k, _ in table]
+        pairs = [(0, 1), (2, 2)]
+        z, _, r = ctx.batch_rho1b([(*w.vacua[i], *w.vacua[j]) for i, j in pairs])
+    for k, (i, j) in enumerate(pairs):
+        zo, ro = kernel_triaxial(w.sp, ham, w.mesh, *w.vacua[i], *w.vacua[j], rho1b=table)
+        sc = np.abs(ro).max()
+        assert np.abs(r[k] - ro.T).max() <= OBS_TOL * sc

@@ -30,3 +30,32 @@ def test_oracle_reproduces_ge76_kernel_files(ge76, i, j):
             mine = k[name][J, JJMAX, JJMAX].real
             ref = gold[jj, f].real
             assert abs(mine - ref) <= 2e-7 * abs(ref) + 1e-12, (J, name, mine, ref)
+
+
+RHO1B_TOL = 2e-9   # the .dens files print 10 decimals
+
+
+@pytest.mark.parametrize("i,j", [(1, 1), (0, 2), (2, 3)])
+def test_oracle_reproduces_ge76_rho1b_files(ge76, i, j):
+    """ZRho1B_Angles / ZRho1B_Integral / Write_ME1B against data/Ge/Rho1B.*.dens."""
+    from oracle.pnamp_oracle import rho1b_table, rho1b_write_me1b
+    g = ge76
+    ham = Hamiltonian(g["e0"], g["t1b"].astype(complex), g["recs"], g["vbar"], g["q2"], g["jops"])
+    mesh = Mesh(1, g["nbet"], 1, g["nfom"], ncosbet=g["ncosbet"])
+    table = rho1b_table(g["sp"])
+    assert [k[:4] for k, _ in table] == g["rho1b_keys"]
+    zres, r = kernel_triaxial(g["sp"], ham, mesh, g["U"][i], g["V"][i], g["U"][j], g["V"][j], iE2=False,
+                              rho1b=table)
+    vals = rho1b_write_me1b(table, zres, r, mesh)
+    assert np.abs(vals - g["rho1b_gold"][i, j]).max() <= RHO1B_TOL, (vals, g["rho1b_gold"][i, j])
+
+
+def test_rho1b_dens_round_trip(tmp_path):
+    from sccm_gb300.formats import read_rho1b_dens, write_rho1b_dens
+    blocks = [(0, 1, 1, 1, 1), (0, 5, 0, 0, 5), (1, 8, 0, 0, 9)]
+    vals = [0.9047578680, 1e-12, 0.0274656496]
+    p = tmp_path / "x.dens"
+    write_rho1b_dens(p, blocks, vals)
+    got = read_rho1b_dens(p)
+    assert set(got) == {(0, 1, 1, 1), (1, 8, 0, 0)}          # the 1e-12 entry is below CHOP
+    assert abs(got[(0, 1, 1, 1)] - vals[0]) < 1e-10
