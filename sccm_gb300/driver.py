@@ -8,14 +8,18 @@
   * `run_pairs`: batches a rank's pairs through the GPU library, projects
     them and writes `kern.*.elem` files through a temporary name and rename
     (the kernel file is the checkpoint: a finished pair is never redone);
-    a manifest lists finished pairs so an interrupted run resumes.
+    a manifest lists finished pairs so an interrupted run resumes. With
+    `rho1b`, each pair's J = 0 one-body density goes to `Rho1B_*.dens` as
+    Write_ME1B writes it (PNAMP_Kernel3D.f90:719, PNAMP_Rho1B.f90:63-91);
+    a pair whose projected norm is below CHOP gets no density file, as there.
 """
 from __future__ import annotations
 
 import json
 import os
 
-from .formats import atomic_write_text, empty_kernels, write_elem_general
+from .formats import atomic_write_text, empty_kernels, write_elem_general, write_rho1b_dens
+from .pnamp import PNAMP_ERR_SMALL_NORM, PnampError
 from .pnamp import PnampContext
 
 
@@ -37,8 +41,12 @@ def elem_name(prefix, q1, q2):
     return f"{prefix}_{q1:03d}_{q2:03d}.elem"
 
 
+def rho1b_name(q1, q2):
+    return f"Rho1B_{q1:03d}_{q2:03d}.dens"
+
+
 def run_pairs(ctx: PnampContext, vacua, pairs, out_dir, prefix="kern", coords=None, batch=8,
-              manifest="manifest.json"):
+              manifest="manifest.json", rho1b=False):
     """Compute and write the kernel files of `pairs` ((q1, q2) 1-based into `vacua`)."""
     os.makedirs(out_dir, exist_ok=True)
     mpath = os.path.join(out_dir, manifest)
@@ -50,8 +58,19 @@ def run_pairs(ctx: PnampContext, vacua, pairs, out_dir, prefix="kern", coords=No
     for s in range(0, len(todo), batch):
         chunk = todo[s:s + batch]
         quads = [(*vacua[q1 - 1], *vacua[q2 - 1]) for (q1, q2) in chunk]
-        zres, status = ctx.batch(quads)
+        if rho1b:
+            zres, status, r1 = ctx.batch_rho1b(quads)
+            blocks = ctx.rho1b_blocks()
+        else:
+            zres, status = ctx.batch(quads)
         for k, (q1, q2) in enumerate(chunk):
+            if rho1b:
+                try:
+                    vals = ctx.project_rho1b(zres[k], r1[k])
+                    atomic_write_text(os.path.join(out_dir, rho1b_name(q1, q2)), write_rho1b_dens, blocks, vals)
+                except PnampError as e:
+                    if e.code != PNAMP_ERR_SMALL_NORM:
+                        raise
             kern = ctx.project(zres[k], chop=True)
             c1 = coords[q1 - 1] if coords is not None else (0.0, 0.0)
             c2 = coords[q2 - 1] if coords is not None else (0.0, 0.0)

@@ -206,11 +206,20 @@ def test_driver_writes_kernel_files_and_resumes(sd, tmp_path):
     from sccm_gb300.driver import pair_list, rank_pairs, run_pairs, elem_name
     from sccm_gb300.formats import read_elem_general
     pairs = pair_list(1, 2, 1, 2, icons=0)
+    from sccm_gb300.driver import rho1b_name
+    from sccm_gb300.formats import read_rho1b_dens
     with ctx_for(sd, sd.mesh) as ctx:
-        done = run_pairs(ctx, sd.vacua, rank_pairs(pairs, 0, 1), str(tmp_path), batch=2)
+        done = run_pairs(ctx, sd.vacua, rank_pairs(pairs, 0, 1), str(tmp_path), batch=2, rho1b=True)
         assert done == pairs
-        z, _ = ctx.batch([(*sd.vacua[0], *sd.vacua[1])])
+        z, _, r1 = ctx.batch_rho1b([(*sd.vacua[0], *sd.vacua[1])])
         kern = ctx.project(z[0])
+        dens = ctx.project_rho1b(z[0], r1[0])
+        blocks = ctx.rho1b_blocks()
+    got = read_rho1b_dens(tmp_path / rho1b_name(1, 2))
+    for b, v in zip(blocks, dens):
+        if b[:4] in got:
+            assert abs(got[b[:4]] - v) <= 1e-10
+    with ctx_for(sd, sd.mesh) as ctx:
         before = os.path.getmtime(tmp_path / elem_name("kern", 1, 2))
         run_pairs(ctx, sd.vacua, pairs, str(tmp_path))          # nothing left to do
         assert os.path.getmtime(tmp_path / elem_name("kern", 1, 2)) == before
