@@ -41,10 +41,10 @@ WORKLOAD = ("pf shell n=40 (Z=4, N=4 valence), 20 seeded deformed vacua -> 210 p
 FORM_TEXT = {"fp64": "plain FP64",
              "df64": "mixed: per-point algebra in double-float (FP32 pairs) on the FP32 pipes, FP64 "
                      "preparation and reductions; norm kernel within 1e-10 of FP64"}
-# DRAM bytes per kernel point of the point kernel (ncu dram__bytes_read + write on a
-# 10,368-point launch, scaled by points; profiles/point_kernel_pf.md): all per-point
+# DRAM bytes per kernel point of the FP64 point kernel (ncu dram__bytes_read + write on a
+# 20,736-point launch, scaled by points; profiles/point_kernel_fp64_pf.md): all per-point
 # matrices live in shared memory or an L2-resident slot, so traffic is tiny.
-TRAFFIC_BYTES_PER_POINT = 609536.0 / 10368.0
+TRAFFIC_BYTES_PER_POINT = 1094912.0 / 20736.0
 # Algorithmic FP64 work per kernel point (pf, n = 40, P_G = 81): rotation,
 # W-solve and T22 partials amortised over the gauge points plus the Pfaffian,
 # T22 inverse and density products: (8+24+16) n^3 / P_G + (10.7+16+40) n^3,
