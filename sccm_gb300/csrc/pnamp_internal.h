@@ -21,15 +21,19 @@ constexpr int kSetupThreads = 256;
 constexpr int kMultiSmemTail = 16;       // dynamic shared bytes after the placement: multi kernel's counter
 
 // One pair record (doubles), all matrices row-major n x n:
-// U0 V0 U1 V1 W Z0 then [det0, det1, status-as-double, pad].
+// U0 V0 U1 V1 W Z0 ZI then [det0, det1, status-as-double, reduced flag, Pf(-c Z0) re, im, pad, pad].
+// ZI = Z0^-1 = U0 V0^-1; with the reduced flag set the point kernel eliminates the n x n
+// matrix c (D X D - ZI) and multiplies by Pf(-c Z0) instead of eliminating the 2n x 2n one.
 struct PairLayout {
-    long long u0, v0, u1, v1, w, z0, dets, stride;
+    long long u0, v0, u1, v1, w, z0, zi, dets, pfz, stride;
     __host__ __device__ void make(int n) {
         long long nn = (long long)n * n;
-        u0 = 0; v0 = nn; u1 = 2 * nn; v1 = 3 * nn; w = 4 * nn; z0 = 5 * nn; dets = 6 * nn;
-        stride = 6 * nn + 4;
+        u0 = 0; v0 = nn; u1 = 2 * nn; v1 = 3 * nn; w = 4 * nn; z0 = 5 * nn; zi = 6 * nn; dets = 7 * nn;
+        pfz = dets + 4;
+        stride = 7 * nn + 8;
     }
 };
+constexpr double kReducedPivotRatio = 1e-6;  // min/max |LU pivot| of V0 for the reduced Pfaffian
 
 // Where the per-point work arrays live: shared memory or the CTA's global slot.
 // Offsets are in bytes (shared) or complex elements (global slot).

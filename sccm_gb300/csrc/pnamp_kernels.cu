@@ -326,7 +326,8 @@ setup_kernel(Params p, const double *__restrict__ uv, double *__restrict__ pairb
     double *Yb = A + nn;
     double *invd = Yb + nn;
     double *red = invd + n;
-    int *perm = reinterpret_cast<int *>(red + 64);
+    zc *vecz = reinterpret_cast<zc *>(red + 64);    // n complex: the Pfaffian's pivot row
+    int *perm = reinterpret_cast<int *>(vecz + n);
     int *sh = perm + n;
     // column-major input -> row-major pair record (U0, V0, U1, V1)
     for (long long t = threadIdx.x; t < 4 * nn; t += blockDim.x) {
@@ -364,13 +365,56 @@ setup_kernel(Params p, const double *__restrict__ uv, double *__restrict__ pairb
         if (threadIdx.x == 0) out[p.pl.dets + (which == 0 ? 1 : 0)] = exp(-0.25 * v[0]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        out[p.pl.dets + 2] = (double)st;
-        out[p.pl.dets + 3] = 0.0;
+    // Reduced Pfaffian data: block elimination of the lower-right block of
+    // S = c [[D X D, -I], [I, -Z0]] gives Pf(S) = Pf(c (D X D - Z0^-1)) Pf(-c Z0), so the point
+    // kernel can eliminate an n x n matrix per point. Kept only when V0 is well conditioned
+    // (Z0^-1 = U0 V0^-1 accurate); otherwise the flag stays 0 and the 2n x 2n form is used.
+    {
+        const double *U0 = out + p.pl.u0, *V0 = out + p.pl.v0, *Z0 = out + p.pl.z0;
+        for (long long t = threadIdx.x; t < nn; t += blockDim.x) {
+            A[t] = V0[t];
+            Yb[t] = U0[t];
+        }
+        __syncthreads();
+        const bool vsing = lu_factor<double>(A, n, n, perm, invd, sh);
+        if (threadIdx.x == 0) {
+            double mx = 0.0, mn = 1e300;
+            for (int k = 0; k < n; ++k) {
+                const double d = fabs(A[k * n + k]);
+                mx = fmax(mx, d);
+                mn = fmin(mn, d);
+            }
+            red[0] = (!vsing && mx > 0.0 && mn >= kReducedPivotRatio * mx) ? 1.0 : 0.0;
+        }
+        __syncthreads();
+        const bool well = red[0] != 0.0;
+        __syncthreads();
+        double ok = 0.0;
+        zc pf = mk(0.0, 0.0);
+        if (well) {
+            row_solve<double>(Yb, n, n, A, n, n, perm, invd);  // U0 V0^-1
+            for (long long t = threadIdx.x; t < nn; t += blockDim.x) out[p.pl.zi + t] = Yb[t];
+            __syncthreads();
+            zc *Sz = reinterpret_cast<zc *>(A);  // n^2 complex over A and Yb
+            for (long long t = threadIdx.x; t < nn; t += blockDim.x) {
+                const int i = (int)(t / n), j = (int)(t % n);
+                Sz[t] = mk(i < j ? -p.cscale * Z0[t] : 0.0, 0.0);
+            }
+            __syncthreads();
+            int under = 0;
+            pf = pfaffian_upper<zc>(Sz, n, vecz, red, sh, under);
+            ok = (under == 0 && zfinite(pf)) ? 1.0 : 0.0;
+        }
+        if (threadIdx.x == 0) {
+            out[p.pl.dets + 2] = (double)st;
+            out[p.pl.dets + 3] = ok;
+            out[p.pl.pfz] = pf.x;
+            out[p.pl.pfz + 1] = pf.y;
+        }
     }
 }
 
-int setup_smem_bytes(int n) { return (2 * n * n + n + 64) * 8 + (n + 8) * 4; }
+int setup_smem_bytes(int n) { return (2 * n * n + n + 64 + 2 * n) * 8 + (n + 8) * 4; }
 
 // The dynamic shared-memory limit of a kernel is a property of the function,
 // shared by every context on the device: it is raised to the device maximum
@@ -458,6 +502,11 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
         const double *gW = pr + p.pl.w, *gZ0 = pr + p.pl.z0;
         const double det0 = pr[p.pl.dets], det1 = pr[p.pl.dets + 1];
         const int pst = (int)pr[p.pl.dets + 2];
+        // reduced Pfaffian (set-up kernel): eliminate c (D X D - Z0^-1), n x n, times Pf(-c Z0)
+        const bool reduced = pr[p.pl.dets + 3] != 0.0;
+        const double *gZi = pr + p.pl.zi;
+        const zc pfz = mk(pr[p.pl.pfz], pr[p.pl.pfz + 1]);
+        const int NP = reduced ? n : N;  // order of the eliminated skew matrix
         double *zout = zres + 2LL * (long long)pair * kNobs * p.n_euler;
         if (pst) {
             for (int io = threadIdx.x; io < kNobs; io += blockDim.x) {
@@ -551,21 +600,23 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
             const Z zep = ephz[lp], zepc = zconj(zep);
             for (int ln = 0; ln < p.nfom; ++ln) {
                 const Z zen = ephz[ln], zenc = zconj(zen);
-                // ---- S = Cscale [[D X D, -I], [I, -Z0]] (upper triangle)
+                // ---- S = Cscale [[D X D, -I], [I, -Z0]] (upper triangle), or for a reduced
+                // pair its Schur complement Cscale (D X D - Z0^-1) (n x n, row stride n)
                 const Z dpp = csz * (zep * zep), dpn = csz * (zep * zen), dnn = csz * (zen * zen);
-                for (int t = threadIdx.x; t < (onishi ? 0 : N * (N - 1) / 2); t += blockDim.x) {
+                for (int t = threadIdx.x; t < (onishi ? 0 : NP * (NP - 1) / 2); t += blockDim.x) {
                     int i, j;
-                    tri_index(t, N, i, j);
+                    tri_index(t, NP, i, j);
                     Z v;
                     if (j < n) {
                         const Z dd_ = (j < h) ? dpp : ((i < h) ? dpn : dnn);
                         v = X[i * n + j] * dd_;
+                        if (reduced) v = v + A::from(mk(-p.cscale * gZi[i * n + j], 0.0));
                     } else if (i < n) {
                         v = (j - n == i) ? mcs : zero;
                     } else {
                         v = A::from(mk(-p.cscale * gZ0[(i - n) * n + (j - n)], 0.0));
                     }
-                    S[i * N + j] = v;
+                    S[i * NP + j] = v;
                 }
                 __syncthreads();
                 int under = 0;
@@ -601,7 +652,8 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     pf = acc[kNobs - 1];
                     __syncthreads();
                 } else {
-                    pf = pfaffian_upper<Z>(S, N, vec, red, sh + 2, under);
+                    pf = pfaffian_upper<Z>(S, NP, vec, red, sh + 2, under);
+                    if (reduced) pf = pf * pfz;  // meaningful in thread 0, like pf
                 }
                 bool sing = false;
                 double *fin = red, *pw = red + kNSlot + 2;
