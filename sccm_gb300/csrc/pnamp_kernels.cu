@@ -162,6 +162,103 @@ __device__ bool lu_factor(T *A, int n, int lda, int *perm, T *invd, int *sh) {
     return sing;
 }
 
+// Y <- Y A^-1 (Y: ny x n, A: n x n, both row-major with leading dimension n) by
+// column-oriented Gauss-Jordan elimination: column operations E reduce A to the
+// identity (A E = I, so E = A^-1), and the same operations applied to the rows of Y
+// give Y A^-1. Step k takes the pivot in row k (largest |A_kc|, c >= k; partial
+// pivoting on A^T), moves column c to k, scales it and removes row k from every other
+// column. Rows < k of A are unit rows by then and are not touched again. Two barriers
+// per step and (n - k - 1 + ny)(n - 1) independent updates per step, against the
+// 2n + n sequential steps of an LU followed by two triangular column sweeps: the
+// elimination is latency-bound at these sizes, so fewer, fuller steps win although
+// the flop count is higher. A holds garbage on return; prow (n) and pinv (1) are
+// shared scratch. Returns true if an exactly zero pivot row was met.
+template <typename T>
+__device__ bool gj_right_solve(T *A, int n, T *Y, int ny, T *prow, T *pinv, int *sh) {
+    const int lane = threadIdx.x & 31;
+    auto search = [&](int k) {  // warp 0: pivot column of row k -> sh[0], zero flag sh[1], pinv[0]
+        double v = -1.0;
+        int idx = 0x7fffffff;
+        for (int j = k + lane; j < n; j += 32) {
+            const double a = sabs1(A[k * n + j]);
+            if (a > v) {
+                v = a;
+                idx = j;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_down_sync(0xffffffffu, v, o);
+            const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+            if (ov > v || (ov == v && oi < idx)) {
+                v = ov;
+                idx = oi;
+            }
+        }
+        if (lane == 0) {
+            const bool none = (idx == 0x7fffffff);  // all NaN: keep column k, report zero
+            const bool z = none || v == 0.0;
+            sh[0] = none ? k : idx;
+            sh[1] = z ? 1 : 0;
+            pinv[0] = z ? szero<T>() : srecip(A[k * n + (none ? k : idx)]);
+        }
+    };
+    bool sing = false;
+    if (threadIdx.x < 32) search(0);
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        const int c = sh[0];
+        if (sh[1]) sing = true;
+        const T pv = pinv[0];
+        // phase 1: each remaining row r gets m_r = M[r][c] / A[k][c] in column k and its old
+        // column k in column c; the pivot row (columns k and c exchanged) goes to prow
+        const int nrT = n - k - 1, nrows = nrT + ny;
+        for (int t = threadIdx.x; t < nrows + n; t += blockDim.x) {
+            if (t < nrows) {
+                T *row = t < nrT ? A + (long long)(k + 1 + t) * n : Y + (long long)(t - nrT) * n;
+                const T a = row[c], b = row[k];
+                row[k] = smul(a, pv);
+                if (c != k) row[c] = b;
+            } else {
+                const int j = t - nrows;
+                prow[j] = (j == c) ? A[k * n + k] : A[k * n + j];
+            }
+        }
+        __syncthreads();
+        // phase 2: M[r][j] -= m_r prow[j] for j != k. Warp 0 takes row k + 1 of A and then
+        // searches its pivot, so the next step needs no extra barrier.
+        if (threadIdx.x < 32) {
+            if (k + 1 < n) {
+                T *row = A + (long long)(k + 1) * n;
+                const T m = row[k];
+                for (int j = lane; j < n; j += 32)
+                    if (j != k) row[j] = sfms(m, prow[j], row[j]);
+                __syncwarp();
+                search(k + 1);
+            }
+        } else {
+            const int nrA = n - k - 2 > 0 ? n - k - 2 : 0;
+            const int total = (nrA + ny) * n, stride = blockDim.x - 32;
+            const int dq = stride / n, dr = stride % n;
+            int rr = (threadIdx.x - 32) / n, j = (threadIdx.x - 32) % n;
+            for (int t = threadIdx.x - 32; t < total; t += stride) {
+                if (j != k) {
+                    T *row = rr < nrA ? A + (long long)(k + 2 + rr) * n : Y + (long long)(rr - nrA) * n;
+                    row[j] = sfms(row[k], prow[j], row[j]);
+                }
+                rr += dq;
+                j += dr;
+                if (j >= n) {
+                    j -= n;
+                    ++rr;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    return sing;
+}
+
 // Y <- Y A^-1 for nr rows of Y (leading dimension ldy), A = P^T L U from lu_factor.
 template <typename T>
 __device__ void row_solve(T *Y, int nr, int ldy, const T *A, int n, int lda, const int *perm,
@@ -668,8 +765,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 }
                 for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) Y[t] = B[t];
                 __syncthreads();
-                sing = lu_factor<Z>(T, n, n, perm, invd, sh);
-                row_solve<Z>(Y, 2 * n, n, T, n, n, perm, invd);
+                sing = gj_right_solve<Z>(T, n, Y, 2 * n, invd, vec, sh);
                 // ---- densities into the Pfaffian's storage, row stride ld
                 {
                     const int dq = blockDim.x / n, dr = blockDim.x % n;
