@@ -45,14 +45,17 @@ FORM_TEXT = {"fp64": "plain FP64",
 # 20,736-point launch, scaled by points; profiles/point_kernel_fp64_pf.md): all per-point
 # matrices live in shared memory or an L2-resident slot, so traffic is tiny.
 TRAFFIC_BYTES_PER_POINT = 1094912.0 / 20736.0
-# Algorithmic FP64 work per kernel point (pf, n = 40, P_G = 81) of the algorithm the
-# kernel runs: rotation, W-solve and T22 partials amortised over the gauge points,
-# (8+24+16) n^3 / P_G, plus per point the Pfaffian of the n x n Schur complement
-# c (D X D - Z0^-1) ((4/3) n^3; the 2n x 2n form of the reference would be (4/3) (2n)^3),
-# the T22 inverse (16 n^3) and the density products (40 n^3), plus the irreducible
-# sparse two-body contraction, 14,442 records x 24 flops.
+# Algorithmic FP64 work per kernel point (pf, n = 40, P_G = 81): the minimal flops of
+# the algorithm the kernel runs (a complex multiply-add = 8 flops, complex x real = 4).
+# Per Euler point, amortised over the gauge points: rotation, W-solve and T22 partials,
+# (8+24+16) n^3 / P_G. Per point: the Pfaffian of the n x n Schur complement
+# c (D X D - Z0^-1), (4/3) n^3 (the reference's 2n x 2n form would be (4/3) (2n)^3);
+# Y T22^-1 for the 2n x n right-hand sides as LU + solves, (8/3 + 16) n^3; the three
+# density products complex x real (U0, V0 are real), 12 n^3; the irreducible sparse
+# two-body contraction, 14,442 records x 24 flops. (The generic count of 40 n^3 for the
+# densities and 16 n^3 for the inverse over-counts this algorithm.)
 def algorithmic_flops_per_point(n, n_gauge, nrec):
-    return (48.0 * n ** 3 / n_gauge + (4.0 / 3.0 + 16.0 + 40.0) * n ** 3) + 24.0 * nrec
+    return (48.0 * n ** 3 / n_gauge + (4.0 / 3.0 + 8.0 / 3.0 + 16.0 + 12.0) * n ** 3) + 24.0 * nrec
 
 
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"

@@ -334,45 +334,53 @@ __device__ __forceinline__ void exch_upper(Z *S, int N, int r, int p, int q) {
     __syncthreads();
 }
 
-// Pfaffian of the N x N skew matrix in the upper triangle of S (row-major),
-// ZPfaffianF (PNAMP_Proj.f90:218-350): at each 2x2 step the largest entry of the
-// remaining upper triangle (row-major scan, first maximum; magnitude max(|re|,|im|))
-// is moved to (r, r+1), the sign flips once per exchange, Pf = 0 when
-// |pivot| <= 1e-13, and the Schur complement is updated in place. The running
-// product is kept in FP64. `vec` holds N scratch values.
+// Pfaffian of the N x N skew matrix in the upper triangle of S (row-major), the
+// 2x2-block elimination of ZPfaffianF (PNAMP_Proj.f90:218-350) with partial instead of
+// global pivoting: at each step the largest entry of row r right of the diagonal (first
+// maximum; magnitude max(|re|,|im|)) is moved to (r, r+1), the sign flips once per
+// exchange, Pf = 0 when |pivot| <= 1e-13, and the Schur complement is updated in place.
+// The running product is kept in FP64. `vec` holds N scratch values; `flag` 2 ints.
 template <class Z>
 __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &underflow) {
+    // Parlett-Reid elimination with partial pivoting: step k takes the largest entry of
+    // row r = 2k right of the diagonal as the 2x2 pivot (swapping its column with c = r + 1),
+    // a one-warp search. (The reference's ZPfaffianF searches the whole remaining upper
+    // triangle, PNAMP_Proj.f90:258-268; both are stable, results agree to rounding.)
     using A = Ar<Z>;
     zc pf = mk(1.0, 0.0);  // running product, meaningful in thread 0
     underflow = 0;
     const int NB = N / 2;
     for (int k = 0; k < NB - 1; ++k) {
-        const int r = 2 * k, c = r + 1, m = N - r;
-        const int T = m * (m - 1) / 2;
-        unsigned long long best = 0ull;
-        int bidx = 0x7fffffff;
-        for (int t = threadIdx.x; t < T; t += blockDim.x) {
-            int i, j;
-            tri_index(t, m, i, j);
-            const unsigned long long key = A::key(S[(r + i) * N + r + j]);
-            if (key > best || bidx == 0x7fffffff) {
-                best = key;
-                bidx = t;
+        const int r = 2 * k, c = r + 1;
+        if (threadIdx.x < 32) {
+            unsigned long long best = 0ull;
+            int bidx = 0x7fffffff;
+            for (int j = c + (int)threadIdx.x; j < N; j += 32) {
+                const unsigned long long key = A::key(S[r * N + j]);
+                if (key > best || bidx == 0x7fffffff) {
+                    best = key;
+                    bidx = j;
+                }
             }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long ob = __shfl_down_sync(0xffffffffu, best, o);
+                const int oi = __shfl_down_sync(0xffffffffu, bidx, o);
+                if (oi != 0x7fffffff && (bidx == 0x7fffffff || ob > best || (ob == best && oi < bidx))) {
+                    best = ob;
+                    bidx = oi;
+                }
+            }
+            if (threadIdx.x == 0) flag[1] = bidx;
         }
-        block_argmax_u64(best, bidx, red);
-        if (bidx == 0x7fffffff) {  // no candidate: cannot happen for T >= 1
+        __syncthreads();
+        const int i2 = flag[1];
+        if (i2 == 0x7fffffff) {  // no candidate: cannot happen for N - c >= 1
             underflow = 2;
             return mk(0.0, 0.0);
         }
-        int i1, i2;
-        tri_index(bidx, m, i1, i2);
-        i1 += r;
-        i2 += r;
-        double phas = 1.0;
-        if (i1 == r) phas = -phas;
+        double phas = -1.0;  // the global-pivot sign rule with i1 = r (PNAMP_Proj.f90:273-275)
         if (i2 == c) phas = -phas;
-        if (i1 != r) exch_upper(S, N, r, r, i1);
         if (i2 != c) exch_upper(S, N, r, c, i2);
         if (threadIdx.x == 0) {  // pivot test, reciprocal and running product by one thread
             const Z ssz = S[r * N + c];
@@ -390,7 +398,7 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &u
             __syncthreads();
             return mk(0.0, 0.0);
         }
-        const Z inv = vec[c];
+    const Z inv = vec[c];
         for (int i = c + 1 + threadIdx.x; i < N; i += blockDim.x) vec[i] = S[c * N + i] * inv;
         __syncthreads();
         const int mm = N - c - 1, TT = mm * (mm - 1) / 2;
