@@ -44,7 +44,7 @@ FORM_TEXT = {"fp64": "plain FP64",
 # DRAM bytes per kernel point of the FP64 point kernel (ncu dram__bytes_read + write on a
 # 20,736-point launch, scaled by points; profiles/point_kernel_fp64_pf.md): all per-point
 # matrices live in shared memory or an L2-resident slot, so traffic is tiny.
-TRAFFIC_BYTES_PER_POINT = 1094912.0 / 20736.0
+TRAFFIC_BYTES_PER_POINT = 532224.0 / 20736.0
 # Algorithmic FP64 work per kernel point (pf, n = 40, P_G = 81): the minimal flops of
 # the algorithm the kernel runs (a complex multiply-add = 8 flops, complex x real = 4).
 # Per Euler point, amortised over the gauge points: rotation, W-solve and T22 partials,
