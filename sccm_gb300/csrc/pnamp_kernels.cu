@@ -259,6 +259,94 @@ __device__ bool gj_right_solve(T *A, int n, T *Y, int ny, T *prow, T *pinv, int 
     return sing;
 }
 
+// gj_right_solve for two independent systems at once: A holds two h x h matrices
+// (compact, the second at A + h*h) and Y two ny x h blocks (the second at Y + ny*h);
+// Y_b <- Y_b A_b^-1 for b = 0, 1 in h steps of two barriers (warp b searches the pivots
+// of system b). prow holds 2h scratch values, pinv 2, sh 4 ints. Returns true if an
+// exactly zero pivot row was met in either system.
+template <typename T>
+__device__ bool gj_right_solve2(T *A, int h, T *Y, int ny, T *prow, T *pinv, int *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int hh = h * h, yh = ny * h;
+    auto search = [&](int b, int k) {  // warp b: pivot column of row k of A_b
+        const T *Ab = A + b * hh;
+        double v = -1.0;
+        int idx = 0x7fffffff;
+        for (int j = k + lane; j < h; j += 32) {
+            const double a = sabs1(Ab[k * h + j]);
+            if (a > v) {
+                v = a;
+                idx = j;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_down_sync(0xffffffffu, v, o);
+            const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+            if (ov > v || (ov == v && oi < idx)) {
+                v = ov;
+                idx = oi;
+            }
+        }
+        if (lane == 0) {
+            const bool none = (idx == 0x7fffffff);
+            const bool z = none || v == 0.0;
+            sh[2 * b] = none ? k : idx;
+            sh[2 * b + 1] = z ? 1 : 0;
+            pinv[b] = z ? szero<T>() : srecip(Ab[k * h + (none ? k : idx)]);
+        }
+    };
+    bool sing = false;
+    if (wid < 2) search(wid, 0);
+    __syncthreads();
+    for (int k = 0; k < h; ++k) {
+        const int c0 = sh[0], c1 = sh[2];
+        if (sh[1] || sh[3]) sing = true;
+        const T pv0 = pinv[0], pv1 = pinv[1];
+        // phase 1 (both systems): m_r = M[r][c] / A[k][c] into column k, old column k into
+        // column c, the exchanged pivot row into prow
+        const int nrT = h - k - 1, nrows = nrT + ny, per1 = nrows + h;
+        for (int t = threadIdx.x; t < 2 * per1; t += blockDim.x) {
+            const int b = t >= per1 ? 1 : 0, u = t - b * per1;
+            const int c = b ? c1 : c0;
+            T *Ab = A + b * hh;
+            if (u < nrows) {
+                T *row = u < nrT ? Ab + (k + 1 + u) * h : Y + b * yh + (u - nrT) * h;
+                const T a = row[c], bb = row[k];
+                row[k] = smul(a, b ? pv1 : pv0);
+                if (c != k) row[c] = bb;
+            } else {
+                const int j = u - nrows;
+                prow[b * h + j] = (j == c) ? Ab[k * h + k] : Ab[k * h + j];
+            }
+        }
+        __syncthreads();
+        // phase 2: M[r][j] -= m_r prow[j] for j != k; warp b takes row k + 1 of A_b, then its pivot
+        if (wid < 2) {
+            if (k + 1 < h) {
+                T *row = A + wid * hh + (k + 1) * h;
+                const T m = row[k];
+                for (int j = lane; j < h; j += 32)
+                    if (j != k) row[j] = sfms(m, prow[wid * h + j], row[j]);
+                __syncwarp();
+                search(wid, k + 1);
+            }
+        } else {
+            const int nrA = h - k - 2 > 0 ? h - k - 2 : 0;
+            const int per2 = (nrA + ny) * h, stride = blockDim.x - 64;
+            for (int t = threadIdx.x - 64; t < 2 * per2; t += stride) {
+                const int b = t >= per2 ? 1 : 0, u = t - b * per2;
+                const int rr = u / h, j = u % h;
+                if (j == k) continue;
+                T *row = rr < nrA ? A + b * hh + (k + 2 + rr) * h : Y + b * yh + (rr - nrA) * h;
+                row[j] = sfms(row[k], prow[b * h + j], row[j]);
+            }
+        }
+        __syncthreads();
+    }
+    return sing;
+}
+
 // Y <- Y A^-1 for nr rows of Y (leading dimension ldy), A = P^T L U from lu_factor.
 template <typename T>
 __device__ void row_solve(T *Y, int nr, int ldy, const T *A, int n, int lda, const int *perm,
@@ -419,6 +507,119 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &u
     return pf;
 }
 
+// Pfaffians of two independent skew h x h matrices stored compactly (upper triangles,
+// row-major, ld h, the second at S + h*h), eliminated together: each step takes both
+// 2x2 pivots (row pivoting as in pfaffian_upper; warp b searches matrix b), so the
+// species-split form of a point needs h/2 - 1 steps for both species. Returns
+// Pf(first) * Pf(second) in thread 0. `vec` holds 2h scratch values, `flag` 4 ints.
+template <class Z>
+__device__ zc pfaffian_upper2(Z *S, int h, Z *vec, int *flag, int &underflow) {
+    using A = Ar<Z>;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int hh = h * h;
+    zc pf = mk(1.0, 0.0);
+    underflow = 0;
+    for (int k = 0; k < h / 2 - 1; ++k) {
+        const int r = 2 * k, c = r + 1;
+        if (wid < 2) {  // warp b: pivot of row r of matrix b
+            const Z *Sb = S + wid * hh;
+            unsigned long long best = 0ull;
+            int bidx = 0x7fffffff;
+            for (int j = c + lane; j < h; j += 32) {
+                const unsigned long long key = A::key(Sb[r * h + j]);
+                if (key > best || bidx == 0x7fffffff) {
+                    best = key;
+                    bidx = j;
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const unsigned long long ob = __shfl_down_sync(0xffffffffu, best, o);
+                const int oi = __shfl_down_sync(0xffffffffu, bidx, o);
+                if (oi != 0x7fffffff && (bidx == 0x7fffffff || ob > best || (ob == best && oi < bidx))) {
+                    best = ob;
+                    bidx = oi;
+                }
+            }
+            if (lane == 0) flag[2 + wid] = bidx;
+        }
+        __syncthreads();
+        const int q0 = flag[2], q1 = flag[3];
+        if (q0 == 0x7fffffff || q1 == 0x7fffffff) {
+            underflow = 2;
+            return mk(0.0, 0.0);
+        }
+        // exchange columns/rows c <-> q of each matrix (exch_upper on both at once)
+        for (int t = threadIdx.x; t < 2 * (h - r); t += blockDim.x) {
+            const int b = t / (h - r), i = r + t % (h - r);
+            const int q = b ? q1 : q0;
+            if (q == c) continue;
+            Z *Sb = S + b * hh;
+            const int pp = c;
+            if (i < pp) {
+                const Z x = Sb[i * h + pp];
+                Sb[i * h + pp] = Sb[i * h + q];
+                Sb[i * h + q] = x;
+            } else if (i > q) {
+                const Z x = Sb[pp * h + i];
+                Sb[pp * h + i] = Sb[q * h + i];
+                Sb[q * h + i] = x;
+            } else if (i > pp && i < q) {
+                const Z x = Sb[pp * h + i];
+                Sb[pp * h + i] = -Sb[i * h + q];
+                Sb[i * h + q] = -x;
+            } else if (i == pp) {
+                Sb[pp * h + q] = -Sb[pp * h + q];
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int f = 0;
+            for (int b = 0; b < 2; ++b) {
+                const Z ssz = S[b * hh + r * h + c];
+                const zc ss = A::to(ssz);
+                const int fb = !zfinite(ss) ? 2 : (!(abs2(ss) > 1.0e-26) ? 1 : 0);
+                if (fb > f) f = fb;
+                if (fb == 0) {
+                    vec[b * h + c] = zrecip(ssz);
+                    const double phas = ((b ? q1 : q0) == c) ? 1.0 : -1.0;
+                    pf = phas * (pf * ss);
+                }
+            }
+            flag[0] = f;
+        }
+        __syncthreads();
+        if (flag[0]) {
+            underflow = flag[0];
+            __syncthreads();
+            return mk(0.0, 0.0);
+        }
+        for (int t = threadIdx.x; t < 2 * (h - c - 1); t += blockDim.x) {
+            const int b = t / (h - c - 1), i = c + 1 + t % (h - c - 1);
+            vec[b * h + i] = S[b * hh + c * h + i] * vec[b * h + c];
+        }
+        __syncthreads();
+        const int mm = h - c - 1, TT = mm * (mm - 1) / 2;
+        for (int t = threadIdx.x; t < 2 * TT; t += blockDim.x) {
+            const int b = t / TT;
+            int i, j;
+            tri_index(t - b * TT, mm, i, j);
+            i += c + 1;
+            j += c + 1;
+            Z *Sb = S + b * hh;
+            const Z *vb = vec + b * h;
+            Z sv = Sb[i * h + j];
+            sv = zfma(vb[i], Sb[r * h + j], sv);
+            sv = zfms(Sb[r * h + i], vb[j], sv);
+            Sb[i * h + j] = sv;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) pf = pf * A::to(S[(h - 2) * h + h - 1]) * A::to(S[hh + (h - 2) * h + h - 1]);
+    __syncthreads();
+    return pf;
+}
+
 // ------------------------------------------------------------------ setup
 __global__ void __launch_bounds__(kSetupThreads)
 setup_kernel(Params p, const double *__restrict__ uv, double *__restrict__ pairbuf) {
@@ -510,11 +711,21 @@ setup_kernel(Params p, const double *__restrict__ uv, double *__restrict__ pairb
             pf = pfaffian_upper<zc>(Sz, n, vecz, red, sh, under);
             ok = (under == 0 && zfinite(pf)) ? 1.0 : 0.0;
         }
+        // species split: U0, V0, U1, V1 without proton-neutron blocks (charge-conserving vacua)
+        // make every per-point matrix block-diagonal by species (protons first, h = n/2 each)
+        int cross = 0;
+        for (long long t = threadIdx.x; t < 4 * nn; t += blockDim.x) {
+            const long long e = t % nn;
+            const int i = (int)(e / n), j = (int)(e % n);
+            if ((i < p.h) != (j < p.h) && out[t] != 0.0) cross = 1;  // U0, V0, U1, V1 lead the record
+        }
+        cross = __syncthreads_or(cross);
         if (threadIdx.x == 0) {
             out[p.pl.dets + 2] = (double)st;
             out[p.pl.dets + 3] = ok;
             out[p.pl.pfz] = pf.x;
             out[p.pl.pfz + 1] = pf.y;
+            out[p.pl.dets + 6] = (ok != 0.0 && !cross) ? 1.0 : 0.0;
         }
     }
 }
@@ -612,6 +823,10 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
         const double *gZi = pr + p.pl.zi;
         const zc pfz = mk(pr[p.pl.pfz], pr[p.pl.pfz + 1]);
         const int NP = reduced ? n : N;  // order of the eliminated skew matrix
+        // species split (set-up kernel): no proton-neutron blocks, so the Schur complement, T22,
+        // the solve and the densities are block-diagonal; both species are eliminated together
+        // on compact h x h blocks
+        const bool split = reduced && pr[p.pl.dets + 6] != 0.0;
         double *zout = zres + 2LL * (long long)pair * kNobs * p.n_euler;
         if (pst) {
             for (int io = threadIdx.x; io < kNobs; io += blockDim.x) {
@@ -708,7 +923,17 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 // ---- S = Cscale [[D X D, -I], [I, -Z0]] (upper triangle), or for a reduced
                 // pair its Schur complement Cscale (D X D - Z0^-1) (n x n, row stride n)
                 const Z dpp = csz * (zep * zep), dpn = csz * (zep * zen), dnn = csz * (zen * zen);
-                for (int t = threadIdx.x; t < (onishi ? 0 : NP * (NP - 1) / 2); t += blockDim.x) {
+                const int Th = h * (h - 1) / 2;
+                for (int t = threadIdx.x; t < (split && !onishi ? 2 * Th : 0); t += blockDim.x) {
+                    const int b = t >= Th ? 1 : 0;
+                    int i, j;
+                    tri_index(t - b * Th, h, i, j);
+                    const int gi = b * h + i, gj = b * h + j;
+                    Z v = X[gi * n + gj] * (b ? dnn : dpp);
+                    v = v + A::from(mk(-p.cscale * gZi[gi * n + gj], 0.0));
+                    S[b * h * h + i * h + j] = v;
+                }
+                for (int t = threadIdx.x; t < (onishi || split ? 0 : NP * (NP - 1) / 2); t += blockDim.x) {
                     int i, j;
                     tri_index(t, NP, i, j);
                     Z v;
@@ -757,13 +982,52 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     pf = acc[kNobs - 1];
                     __syncthreads();
                 } else {
-                    pf = pfaffian_upper<Z>(S, NP, vec, red, sh + 2, under);
+                    if (split)
+                        pf = pfaffian_upper2<Z>(S, h, vec, sh + 2, under);
+                    else
+                        pf = pfaffian_upper<Z>(S, NP, vec, red, sh + 2, under);
                     if (reduced) pf = pf * pfz;  // meaningful in thread 0, like pf
                 }
                 bool sing = false;
                 double *fin = red, *pw = red + kNSlot + 2;
                 if (!p.norm_only) {  // uniform over the block: norm-only launches skip the densities
                 // ---- T22(phi) and right-hand sides
+                if (split) {  // compact species blocks: T_b (h x h), Y_b = [R V1; R* U1] rows and columns of b
+                    for (int t = threadIdx.x; t < 2 * h * h; t += blockDim.x) {
+                        const int b = t >= h * h ? 1 : 0, e = t - b * h * h, i = e / h, j = e % h;
+                        const int g = (b * h + i) * n + b * h + j;
+                        Z s = zep * P[g];
+                        s = zfma(zen, P[nn + g], s);
+                        s = zfma(zepc, P[2 * nn + g], s);
+                        s = zfma(zenc, P[3 * nn + g], s);
+                        T[t] = s;
+                    }
+                    for (int t = threadIdx.x; t < 4 * h * h; t += blockDim.x) {
+                        const int b = t >= 2 * h * h ? 1 : 0, e = t - 2 * b * h * h, r = e / h, j = e % h;
+                        const int grow = r < h ? b * h + r : n + b * h + (r - h);
+                        Y[t] = B[grow * n + b * h + j];
+                    }
+                    __syncthreads();
+                    sing = gj_right_solve2<Z>(T, h, Y, 2 * h, invd, vec, sh);
+                    // densities of each species block (rows and columns of b), zero across species
+                    for (int q = 0; q < 3; ++q) {
+                        const R *Mq = (q == 1) ? U0t : V0t;
+                        Z *Sq = S + q * n * ld;
+                        for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+                            const int i = t / n, j = t % n, b = i < h ? 0 : 1;
+                            const int bj = j < h ? 0 : 1;
+                            Z sv = zero;
+                            if (b == bj) {
+                                const Z *Yr = Y + 2 * b * h * h + ((q == 2 ? h : 0) + i - b * h) * h;
+                                const R *M = Mq + (b * h) * n + j;
+                                for (int k = 0; k < h; ++k) sv = rfma(M[k * n], Yr[k], sv);
+                                const Z di = b ? zen : zep;
+                                sv = (q == 2) ? -(zconj(di) * sv) : di * sv;
+                            }
+                            Sq[i * ld + j] = sv;
+                        }
+                    }
+                } else {
                 for (int t = threadIdx.x; t < nn; t += blockDim.x) {
                     Z s = zep * P[t];
                     s = zfma(zen, P[nn + t], s);
@@ -798,6 +1062,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         }
                     }
                 }
+                }  // split
                 __syncthreads();
                 // K01_ij (i < j) at Kc[i ld + j], K10_ij at Kc[j ld + i]
                 for (int t = threadIdx.x; t < n * (n - 1) / 2; t += blockDim.x) {
