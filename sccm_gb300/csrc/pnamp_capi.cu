@@ -298,6 +298,25 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
         if (a < 0 || b < 0 || c < 0 || d < 0 || a >= n || b >= n || c >= n || d >= n) return PNAMP_ERR_ARG;
         rec_idx[e] = (uint32_t)a | ((uint32_t)b << 8) | ((uint32_t)c << 16) | ((uint32_t)d << 24);
     }
+    // proton-neutron records (a, c protons; b, d neutrons) last: for species-split pairs half
+    // of their terms vanish and the point kernel takes a shorter path over that range
+    int nrec_gen = 0;
+    {
+        std::vector<uint32_t> gi, pi;
+        std::vector<double> gv, pv;
+        for (int e = 0; e < h->nrec; ++e) {
+            const int a = rec_idx[e] & 0xff, b = (rec_idx[e] >> 8) & 0xff, c = (rec_idx[e] >> 16) & 0xff,
+                      d = rec_idx[e] >> 24;
+            const bool pn = a < hh && b >= hh && c < hh && d >= hh;
+            (pn ? pi : gi).push_back(rec_idx[e]);
+            (pn ? pv : gv).push_back(rec_v[e]);
+        }
+        nrec_gen = (int)gi.size();
+        gi.insert(gi.end(), pi.begin(), pi.end());
+        gv.insert(gv.end(), pv.begin(), pv.end());
+        rec_idx.swap(gi);
+        rec_v.swap(gv);
+    }
     // one-body tables
     std::vector<int> t1b_idx;
     std::vector<double> t1b_val;
@@ -367,6 +386,7 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
     p.nblk = (int)blk_start.size();
     p.rot_elems = rot;
     p.nrec = h->nrec;
+    p.nrec_gen = nrec_gen;
     p.pl.make(n);
     c->core_prot = sp->core_prot;
     c->core_neut = sp->core_neut;
@@ -386,6 +406,17 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
     UP(row_blk, p.row_blk);
     UP(twom, p.twom);
     UP(euler, p.euler);
+    {
+        std::vector<double> gph(2 * (size_t)m->nfom * m->nfom);
+        const double twopi = 6.283185307179586476925287;
+        for (int lp = 0; lp < m->nfom; ++lp)
+            for (int ln = 0; ln < m->nfom; ++ln) {
+                const double a = -(twopi * lp / m->nfom * sp->nprot + twopi * ln / m->nfom * sp->nneut);
+                gph[2 * (lp * m->nfom + ln)] = std::cos(a);
+                gph[2 * (lp * m->nfom + ln) + 1] = std::sin(a);
+            }
+        UP(gph, p.gphase);
+    }
     UP(fact, p.fact);
     UP(rec_idx, p.rec_idx);
     UP(rec_v, p.rec_v);

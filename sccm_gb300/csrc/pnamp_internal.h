@@ -81,9 +81,11 @@ struct Params {
     int nblk, rot_elems;
     const int *blk_start, *blk_size, *blk_tj, *blk_roff, *row_blk, *twom;
     const double *euler;       // [n_euler][4] alpha, beta, gamma, weight
+    const double *gphase;      // [nfom][nfom] complex e^{-i (phi_lp Z + phi_ln N)}, the projection phase
     const double *fact;        // k!, k = 0..23
     // Hamiltonian two-body list
     int nrec;
+    int nrec_gen;              // records [0, nrec_gen): general; [nrec_gen, nrec): a, c protons and b, d neutrons
     const uint32_t *rec_idx;   // packed 8-bit a,b,c,d (0-based)
     const double *rec_v;
     const dd *rec_vd;          // rec_v as double-float (df64 form)

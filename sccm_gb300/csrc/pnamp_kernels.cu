@@ -1166,16 +1166,35 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         t = rfma(quarter, u, t);
                         e2 = rfma(v, t, e2);
                     };
+                    // proton-neutron records of a species-split pair: rho_li, rho_kj, rho_jk, rho_il
+                    // and both pairing tensors cross the species and vanish
+                    auto rec_pn = [&](uint32_t pk, R v) {
+                        const int i = pk & 0xff, j = (pk >> 8) & 0xff, k = (pk >> 16) & 0xff, l = pk >> 24;
+                        Z t = rho[k * ld + i] * rho[l * ld + j];
+                        if (i + j != k + l) t = zfma(rho[i * ld + k], rho[j * ld + l], t);
+                        e2 = rfma(v, t, e2);
+                    };
                     const int stride = blockDim.x;
-                    for (int e = threadIdx.x; e < p.nrec; e += 2 * stride) {
+                    const int ngen = split ? p.nrec_gen : p.nrec;
+                    for (int e = threadIdx.x; e < ngen; e += 2 * stride) {
+                        const int e1 = e + stride;
+                        const uint32_t pk0 = p.rec_idx[e];
+                        const R v0 = A::pick(p.rec_v, p.rec_vd, e);
+                        const bool two = e1 < ngen;
+                        const uint32_t pk1 = two ? p.rec_idx[e1] : 0u;
+                        const R v1 = two ? A::pick(p.rec_v, p.rec_vd, e1) : A::real(0.0);
+                        rec(pk0, v0);
+                        if (two) rec(pk1, v1);
+                    }
+                    for (int e = ngen + threadIdx.x; e < p.nrec; e += 2 * stride) {
                         const int e1 = e + stride;
                         const uint32_t pk0 = p.rec_idx[e];
                         const R v0 = A::pick(p.rec_v, p.rec_vd, e);
                         const bool two = e1 < p.nrec;
                         const uint32_t pk1 = two ? p.rec_idx[e1] : 0u;
                         const R v1 = two ? A::pick(p.rec_v, p.rec_vd, e1) : A::real(0.0);
-                        rec(pk0, v0);
-                        if (two) rec(pk1, v1);
+                        rec_pn(pk0, v0);
+                        if (two) rec_pn(pk1, v1);
                     }
                     const zc e2c = A::to(e2);
                     put(0, e2c.x);
@@ -1223,7 +1242,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         }
                         return fin[slot];
                     };
-                    const zc zph = expi(-(twopi * lp / p.nfom * p.nprot + twopi * ln / p.nfom * p.nneut));
+                    const zc zph = mk(p.gphase[2 * (lp * p.nfom + ln)], p.gphase[2 * (lp * p.nfom + ln) + 1]);
                     const zc norm = onishi ? pf : (p.vacfac * det0 * det1) * (pf * zph);
                     const zc trp = mk(get(10), get(11)), trm = mk(get(12), get(13)), trz = mk(get(14), get(15));
                     const zc j2 = mk(get(16) + get(8), get(17) + get(9)) + trp * trm + trz * trz;

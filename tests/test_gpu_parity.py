@@ -261,3 +261,26 @@ def test_rho1b_blocks_with_two_radial_orbits_match_oracle():
         zo, ro = kernel_triaxial(w.sp, ham, w.mesh, *w.vacua[i], *w.vacua[j], rho1b=table)
         sc = np.abs(ro).max()
         assert np.abs(r[k] - ro.T).max() <= OBS_TOL * sc
+
+
+def test_quasiparticle_basis_change_takes_general_path():
+    """(U C, V C) with C orthogonal is the same vacuum. A C that mixes proton and neutron
+    quasiparticle columns gives U, V with proton-neutron blocks, so the kernels leave the
+    species-split form for the general one; the results must not change."""
+    from scipy.linalg import expm
+    w = make_workload("pf", 2, Mesh(2, 3, 2, 3), seed=515)
+    n = w.sp.nlev
+    rng = np.random.default_rng(9)
+    G = rng.normal(0.0, 0.3, (n, n))
+    C = expm(G - G.T)
+    mixed = [(U @ C, V @ C) for U, V in w.vacua]
+    assert np.abs(mixed[0][0][: n // 2, n // 2:]).max() > 1e-3
+    pairs = [(0, 1), (1, 1)]
+    with ctx_for(w, w.mesh) as ctx:
+        z_ref, _ = ctx.batch([(*w.vacua[i], *w.vacua[j]) for i, j in pairs])
+        z_mix, _ = ctx.batch([(*mixed[i], *mixed[j]) for i, j in pairs])
+    for k in range(len(pairs)):
+        for io in range(19):
+            sc = np.abs(z_ref[k][:, io]).max()
+            tol = NORM_TOL if io == 0 else OBS_TOL
+            assert np.abs(z_mix[k][:, io] - z_ref[k][:, io]).max() <= tol * max(sc, 1e-300), io
