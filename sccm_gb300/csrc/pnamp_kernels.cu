@@ -162,6 +162,16 @@ __device__ bool lu_factor(T *A, int n, int lda, int *perm, T *invd, int *sh) {
     return sing;
 }
 
+// A warp-aligned group of the CTA's threads with its own named barrier (bar.sync id,
+// count; id 0 with the whole CTA is __syncthreads). Lets two independent latency-bound
+// eliminations run at the same time on disjoint warps.
+struct Grp {
+    int tid, nthr, wid, bar;
+};
+__device__ __forceinline__ void gsync(const Grp &g) {
+    asm volatile("bar.sync %0, %1;" ::"r"(g.bar), "r"(g.nthr) : "memory");
+}
+
 // Y <- Y A^-1 (Y: ny x n, A: n x n, both row-major with leading dimension n) by
 // column-oriented Gauss-Jordan elimination: column operations E reduce A to the
 // identity (A E = I, so E = A^-1), and the same operations applied to the rows of Y
@@ -259,14 +269,15 @@ __device__ bool gj_right_solve(T *A, int n, T *Y, int ny, T *prow, T *pinv, int 
     return sing;
 }
 
-// gj_right_solve for two independent systems at once: A holds two h x h matrices
+// gj_right_solve for two independent systems at once, by the thread group g (at least
+// 3 warps; warps 0 and 1 of the group search the pivots): A holds two h x h matrices
 // (compact, the second at A + h*h) and Y two ny x h blocks (the second at Y + ny*h);
 // Y_b <- Y_b A_b^-1 for b = 0, 1 in h steps of two barriers (warp b searches the pivots
 // of system b). prow holds 2h scratch values, pinv 2, sh 4 ints. Returns true if an
 // exactly zero pivot row was met in either system.
 template <typename T>
-__device__ bool gj_right_solve2(T *A, int h, T *Y, int ny, T *prow, T *pinv, int *sh) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+__device__ bool gj_right_solve2(const Grp &g, T *A, int h, T *Y, int ny, T *prow, T *pinv, int *sh) {
+    const int lane = g.tid & 31, wid = g.wid;
     const int hh = h * h, yh = ny * h;
     auto search = [&](int b, int k) {  // warp b: pivot column of row k of A_b
         const T *Ab = A + b * hh;
@@ -298,7 +309,7 @@ __device__ bool gj_right_solve2(T *A, int h, T *Y, int ny, T *prow, T *pinv, int
     };
     bool sing = false;
     if (wid < 2) search(wid, 0);
-    __syncthreads();
+    gsync(g);
     for (int k = 0; k < h; ++k) {
         const int c0 = sh[0], c1 = sh[2];
         if (sh[1] || sh[3]) sing = true;
@@ -306,7 +317,7 @@ __device__ bool gj_right_solve2(T *A, int h, T *Y, int ny, T *prow, T *pinv, int
         // phase 1 (both systems): m_r = M[r][c] / A[k][c] into column k, old column k into
         // column c, the exchanged pivot row into prow
         const int nrT = h - k - 1, nrows = nrT + ny, per1 = nrows + h;
-        for (int t = threadIdx.x; t < 2 * per1; t += blockDim.x) {
+        for (int t = g.tid; t < 2 * per1; t += g.nthr) {
             const int b = t >= per1 ? 1 : 0, u = t - b * per1;
             const int c = b ? c1 : c0;
             T *Ab = A + b * hh;
@@ -320,7 +331,7 @@ __device__ bool gj_right_solve2(T *A, int h, T *Y, int ny, T *prow, T *pinv, int
                 prow[b * h + j] = (j == c) ? Ab[k * h + k] : Ab[k * h + j];
             }
         }
-        __syncthreads();
+        gsync(g);
         // phase 2: M[r][j] -= m_r prow[j] for j != k; warp b takes row k + 1 of A_b, then its pivot
         if (wid < 2) {
             if (k + 1 < h) {
@@ -333,8 +344,8 @@ __device__ bool gj_right_solve2(T *A, int h, T *Y, int ny, T *prow, T *pinv, int
             }
         } else {
             const int nrA = h - k - 2 > 0 ? h - k - 2 : 0;
-            const int per2 = (nrA + ny) * h, stride = blockDim.x - 64;
-            for (int t = threadIdx.x - 64; t < 2 * per2; t += stride) {
+            const int per2 = (nrA + ny) * h, stride = g.nthr - 64;
+            for (int t = g.tid - 64; t < 2 * per2; t += stride) {
                 const int b = t >= per2 ? 1 : 0, u = t - b * per2;
                 const int rr = u / h, j = u % h;
                 if (j == k) continue;
@@ -342,7 +353,7 @@ __device__ bool gj_right_solve2(T *A, int h, T *Y, int ny, T *prow, T *pinv, int
                 row[j] = sfms(row[k], prow[b * h + j], row[j]);
             }
         }
-        __syncthreads();
+        gsync(g);
     }
     return sing;
 }
@@ -508,14 +519,15 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &u
 }
 
 // Pfaffians of two independent skew h x h matrices stored compactly (upper triangles,
-// row-major, ld h, the second at S + h*h), eliminated together: each step takes both
-// 2x2 pivots (row pivoting as in pfaffian_upper; warp b searches matrix b), so the
-// species-split form of a point needs h/2 - 1 steps for both species. Returns
-// Pf(first) * Pf(second) in thread 0. `vec` holds 2h scratch values, `flag` 4 ints.
+// row-major, ld h, the second at S + h*h), eliminated together by the thread group g:
+// each step takes both 2x2 pivots (row pivoting as in pfaffian_upper; warp b of the group
+// searches matrix b), so the species-split form of a point needs h/2 - 1 steps for both
+// species. Returns Pf(first) * Pf(second) in the group's thread 0. `vec` holds 2h scratch
+// values, `flag` 4 ints.
 template <class Z>
-__device__ zc pfaffian_upper2(Z *S, int h, Z *vec, int *flag, int &underflow) {
+__device__ zc pfaffian_upper2(const Grp &g, Z *S, int h, Z *vec, int *flag, int &underflow) {
     using A = Ar<Z>;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int lane = g.tid & 31, wid = g.wid;
     const int hh = h * h;
     zc pf = mk(1.0, 0.0);
     underflow = 0;
@@ -543,14 +555,14 @@ __device__ zc pfaffian_upper2(Z *S, int h, Z *vec, int *flag, int &underflow) {
             }
             if (lane == 0) flag[2 + wid] = bidx;
         }
-        __syncthreads();
+        gsync(g);
         const int q0 = flag[2], q1 = flag[3];
         if (q0 == 0x7fffffff || q1 == 0x7fffffff) {
             underflow = 2;
             return mk(0.0, 0.0);
         }
         // exchange columns/rows c <-> q of each matrix (exch_upper on both at once)
-        for (int t = threadIdx.x; t < 2 * (h - r); t += blockDim.x) {
+        for (int t = g.tid; t < 2 * (h - r); t += g.nthr) {
             const int b = t / (h - r), i = r + t % (h - r);
             const int q = b ? q1 : q0;
             if (q == c) continue;
@@ -572,8 +584,8 @@ __device__ zc pfaffian_upper2(Z *S, int h, Z *vec, int *flag, int &underflow) {
                 Sb[pp * h + q] = -Sb[pp * h + q];
             }
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
+        gsync(g);
+        if (g.tid == 0) {
             int f = 0;
             for (int b = 0; b < 2; ++b) {
                 const Z ssz = S[b * hh + r * h + c];
@@ -588,19 +600,19 @@ __device__ zc pfaffian_upper2(Z *S, int h, Z *vec, int *flag, int &underflow) {
             }
             flag[0] = f;
         }
-        __syncthreads();
+        gsync(g);
         if (flag[0]) {
             underflow = flag[0];
-            __syncthreads();
+            gsync(g);
             return mk(0.0, 0.0);
         }
-        for (int t = threadIdx.x; t < 2 * (h - c - 1); t += blockDim.x) {
+        for (int t = g.tid; t < 2 * (h - c - 1); t += g.nthr) {
             const int b = t / (h - c - 1), i = c + 1 + t % (h - c - 1);
             vec[b * h + i] = S[b * hh + c * h + i] * vec[b * h + c];
         }
-        __syncthreads();
+        gsync(g);
         const int mm = h - c - 1, TT = mm * (mm - 1) / 2;
-        for (int t = threadIdx.x; t < 2 * TT; t += blockDim.x) {
+        for (int t = g.tid; t < 2 * TT; t += g.nthr) {
             const int b = t / TT;
             int i, j;
             tri_index(t - b * TT, mm, i, j);
@@ -613,10 +625,10 @@ __device__ zc pfaffian_upper2(Z *S, int h, Z *vec, int *flag, int &underflow) {
             sv = zfms(Sb[r * h + i], vb[j], sv);
             Sb[i * h + j] = sv;
         }
-        __syncthreads();
+        gsync(g);
     }
-    if (threadIdx.x == 0) pf = pf * A::to(S[(h - 2) * h + h - 1]) * A::to(S[hh + (h - 2) * h + h - 1]);
-    __syncthreads();
+    if (g.tid == 0) pf = pf * A::to(S[(h - 2) * h + h - 1]) * A::to(S[hh + (h - 2) * h + h - 1]);
+    gsync(g);
     return pf;
 }
 
@@ -923,15 +935,54 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 // ---- S = Cscale [[D X D, -I], [I, -Z0]] (upper triangle), or for a reduced
                 // pair its Schur complement Cscale (D X D - Z0^-1) (n x n, row stride n)
                 const Z dpp = csz * (zep * zep), dpn = csz * (zep * zen), dnn = csz * (zen * zen);
-                const int Th = h * (h - 1) / 2;
-                for (int t = threadIdx.x; t < (split && !onishi ? 2 * Th : 0); t += blockDim.x) {
-                    const int b = t >= Th ? 1 : 0;
-                    int i, j;
-                    tri_index(t - b * Th, h, i, j);
-                    const int gi = b * h + i, gj = b * h + j;
-                    Z v = X[gi * n + gj] * (b ? dnn : dpp);
-                    v = v + A::from(mk(-p.cscale * gZi[gi * n + gj], 0.0));
-                    S[b * h * h + i * h + j] = v;
+                // species split: warps 0-3 build and eliminate the two Schur-complement blocks
+                // while warps 4-15 build T22 and Y and run the Gauss-Jordan solve (named barriers
+                // 1 and 2); both are latency-bound, so running them side by side hides one behind
+                // the other. One CTA barrier joins them before the densities.
+                const bool conc = split && !onishi;
+                int under = 0;
+                zc pf = mk(0.0, 0.0);
+                bool sing = false;
+                if (conc) {
+                    constexpr int kPfWarps = 4;
+                    if (wid < kPfWarps) {
+                        const Grp g{(int)threadIdx.x, kPfWarps * 32, wid, 1};
+                        const int Th = h * (h - 1) / 2;
+                        for (int t = g.tid; t < 2 * Th; t += g.nthr) {
+                            const int b = t >= Th ? 1 : 0;
+                            int i, j;
+                            tri_index(t - b * Th, h, i, j);
+                            const int gi = b * h + i, gj = b * h + j;
+                            Z v = X[gi * n + gj] * (b ? dnn : dpp);
+                            v = v + A::from(mk(-p.cscale * gZi[gi * n + gj], 0.0));
+                            S[b * h * h + i * h + j] = v;
+                        }
+                        gsync(g);
+                        pf = pfaffian_upper2<Z>(g, S, h, vec, sh, under);
+                        pf = pf * pfz;  // meaningful in thread 0
+                    } else if (!p.norm_only) {
+                        const Grp g{(int)threadIdx.x - kPfWarps * 32, (int)blockDim.x - kPfWarps * 32,
+                                    wid - kPfWarps, 2};
+                        for (int t = g.tid; t < 2 * h * h; t += g.nthr) {
+                            const int b = t >= h * h ? 1 : 0, e = t - b * h * h, i = e / h, j = e % h;
+                            const int gg = (b * h + i) * n + b * h + j;
+                            Z sv = zep * P[gg];
+                            sv = zfma(zen, P[nn + gg], sv);
+                            sv = zfma(zepc, P[2 * nn + gg], sv);
+                            sv = zfma(zenc, P[3 * nn + gg], sv);
+                            T[t] = sv;
+                        }
+                        for (int t = g.tid; t < 4 * h * h; t += g.nthr) {
+                            const int b = t >= 2 * h * h ? 1 : 0, e = t - 2 * b * h * h, r = e / h, j = e % h;
+                            const int grow = r < h ? b * h + r : n + b * h + (r - h);
+                            Y[t] = B[grow * n + b * h + j];
+                        }
+                        gsync(g);
+                        const bool sg = gj_right_solve2<Z>(g, T, h, Y, 2 * h, invd, vec + 2 * h, sh + 4);
+                        if (g.tid == 0) sh[4] = sg ? 1 : 0;
+                    }
+                    __syncthreads();
+                    if (!p.norm_only) sing = sh[4] != 0;
                 }
                 for (int t = threadIdx.x; t < (onishi || split ? 0 : NP * (NP - 1) / 2); t += blockDim.x) {
                     int i, j;
@@ -948,10 +999,9 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     }
                     S[i * NP + j] = v;
                 }
-                __syncthreads();
-                int under = 0;
-                zc pf;
-                if (onishi) {
+                if (!conc) __syncthreads();
+                if (conc) {
+                } else if (onishi) {
                     // Onishi (PNAMP_Onishi.f90:21-37): sqrt(det(Ubar^T U0 + Vbar^T V0)),
                     // Ubar = R U1, Vbar = conj(R) V1 at phi = 0; LU determinant, principal root
                     zc *Bm = reinterpret_cast<zc *>(S);
@@ -982,18 +1032,14 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     pf = acc[kNobs - 1];
                     __syncthreads();
                 } else {
-                    if (split)
-                        pf = pfaffian_upper2<Z>(S, h, vec, sh + 2, under);
-                    else
-                        pf = pfaffian_upper<Z>(S, NP, vec, red, sh + 2, under);
+                    pf = pfaffian_upper<Z>(S, NP, vec, red, sh + 2, under);
                     if (reduced) pf = pf * pfz;  // meaningful in thread 0, like pf
                 }
-                bool sing = false;
                 double *fin = red, *pw = red + kNSlot + 2;
                 if (!p.norm_only) {  // uniform over the block: norm-only launches skip the densities
                 // ---- T22(phi) and right-hand sides
                 if (split) {  // compact species blocks: T_b (h x h), Y_b = [R V1; R* U1] rows and columns of b
-                    for (int t = threadIdx.x; t < 2 * h * h; t += blockDim.x) {
+                    for (int t = threadIdx.x; t < (conc ? 0 : 2 * h * h); t += blockDim.x) {
                         const int b = t >= h * h ? 1 : 0, e = t - b * h * h, i = e / h, j = e % h;
                         const int g = (b * h + i) * n + b * h + j;
                         Z s = zep * P[g];
@@ -1002,13 +1048,16 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         s = zfma(zenc, P[3 * nn + g], s);
                         T[t] = s;
                     }
-                    for (int t = threadIdx.x; t < 4 * h * h; t += blockDim.x) {
+                    for (int t = threadIdx.x; t < (conc ? 0 : 4 * h * h); t += blockDim.x) {
                         const int b = t >= 2 * h * h ? 1 : 0, e = t - 2 * b * h * h, r = e / h, j = e % h;
                         const int grow = r < h ? b * h + r : n + b * h + (r - h);
                         Y[t] = B[grow * n + b * h + j];
                     }
-                    __syncthreads();
-                    sing = gj_right_solve2<Z>(T, h, Y, 2 * h, invd, vec, sh);
+                    if (!conc) {  // (Onishi norm) the whole CTA solves after the norm
+                        __syncthreads();
+                        const Grp gall{(int)threadIdx.x, (int)blockDim.x, wid, 0};
+                        sing = gj_right_solve2<Z>(gall, T, h, Y, 2 * h, invd, vec, sh);
+                    }
                     // densities of each species block (rows and columns of b), zero across species
                     for (int q = 0; q < 3; ++q) {
                         const R *Mq = (q == 1) ? U0t : V0t;
