@@ -1058,23 +1058,31 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         const Grp gall{(int)threadIdx.x, (int)blockDim.x, wid, 0};
                         sing = gj_right_solve2<Z>(gall, T, h, Y, 2 * h, invd, vec, sh);
                     }
-                    // densities of each species block (rows and columns of b), zero across species
-                    for (int q = 0; q < 3; ++q) {
-                        const R *Mq = (q == 1) ? U0t : V0t;
-                        Z *Sq = S + q * n * ld;
-                        for (int t = threadIdx.x; t < nn; t += blockDim.x) {
-                            const int i = t / n, j = t % n, b = i < h ? 0 : 1;
-                            const int bj = j < h ? 0 : 1;
-                            Z sv = zero;
-                            if (b == bj) {
-                                const Z *Yr = Y + 2 * b * h * h + ((q == 2 ? h : 0) + i - b * h) * h;
-                                const R *M = Mq + (b * h) * n + j;
-                                for (int k = 0; k < h; ++k) sv = rfma(M[k * n], Yr[k], sv);
-                                const Z di = b ? zen : zep;
-                                sv = (q == 2) ? -(zconj(di) * sv) : di * sv;
-                            }
-                            Sq[i * ld + j] = sv;
+                    // densities of each species block in one pass (rho, kappa10 and kappa01 of an
+                    // entry share the loads of Y and V0^T), and zeros across the species
+                    for (int t = threadIdx.x; t < 2 * h * h; t += blockDim.x) {
+                        const int b = t >= h * h ? 1 : 0, e = t - b * h * h, i = e / h, j = e % h;
+                        const Z *Yt = Y + 2 * b * h * h + i * h;   // R V1 T22^-1 rows of species b
+                        const Z *Yb = Yt + h * h;                  // R* U1 T22^-1 rows
+                        const R *Mv = V0t + (b * h) * n + b * h + j, *Mu = U0t + (b * h) * n + b * h + j;
+                        Z sr = zero, s10 = zero, s01 = zero;
+                        for (int k = 0; k < h; ++k) {
+                            const Z yt = Yt[k];
+                            const R mv = Mv[k * n];
+                            sr = rfma(mv, yt, sr);
+                            s10 = rfma(Mu[k * n], yt, s10);
+                            s01 = rfma(mv, Yb[k], s01);
                         }
+                        const Z di = b ? zen : zep;
+                        const int o = (b * h + i) * ld + b * h + j;
+                        S[o] = di * sr;
+                        S[n * ld + o] = di * s10;
+                        S[2 * n * ld + o] = -(zconj(di) * s01);
+                    }
+                    for (int t = threadIdx.x; t < 6 * h * h; t += blockDim.x) {  // cross-species zeros
+                        const int q = t / (2 * h * h), e = t % (2 * h * h), b = e >= h * h ? 1 : 0;
+                        const int i = (e - b * h * h) / h, j = (e - b * h * h) % h;
+                        S[q * n * ld + (b * h + i) * ld + (1 - b) * h + j] = zero;
                     }
                 } else {
                 for (int t = threadIdx.x; t < nn; t += blockDim.x) {
@@ -1123,41 +1131,53 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 __syncthreads();
                 // ---- observables. Final sums land in red[0..kNSlot); the energy and <J^2>
                 // sums, spread over all warps, leave per-warp partials in red[kNSlot + ..].
-                if (wid == 0) {  // traces of rho: warp 0 alone
-                    double z0 = 0, z1 = 0, n0 = 0, n1 = 0, j0 = 0, j1 = 0, p0 = 0, p1 = 0, m0 = 0, m1 = 0, c0 = 0,
-                           c1 = 0, t0 = 0, t1 = 0;
-                    for (int a = lane; a < n; a += 32) {
-                        const zc d = A::to(rho[a * ld + a]);
-                        if (a < h) { z0 += d.x; z1 += d.y; }
-                        else { n0 += d.x; n1 += d.y; }
-                        j0 = fma(p.obs.jj1[a], d.x, j0);
-                        j1 = fma(p.obs.jj1[a], d.y, j1);
-                        const double jpa = p.obs.jp[a], jma = p.obs.jm[a], mza = p.obs.mz[a];
-                        if (jpa != 0.0) {
-                            const zc r = A::to(rho[(a + 1) * ld + a]);
-                            p0 = fma(jpa, r.x, p0);
-                            p1 = fma(jpa, r.y, p1);
+                // traces of rho, spread over warps 0 (species traces, sum j(j+1) rho_aa), 11 (J+, J-,
+                // Jz) and 12 (one-body energy) so that no warp starts the energy loop much later
+                if (wid == 0 || wid == kNTrace + 1 || wid == kNTrace + 2) {
+                    double v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
+                    if (wid == 0) {
+                        for (int a = lane; a < n; a += 32) {
+                            const zc d = A::to(rho[a * ld + a]);
+                            if (a < h) { v0 += d.x; v1 += d.y; }
+                            else { v2 += d.x; v3 += d.y; }
+                            v4 = fma(p.obs.jj1[a], d.x, v4);
+                            v5 = fma(p.obs.jj1[a], d.y, v5);
                         }
-                        if (jma != 0.0) {
-                            const zc r = A::to(rho[(a - 1) * ld + a]);
-                            m0 = fma(jma, r.x, m0);
-                            m1 = fma(jma, r.y, m1);
+                    } else if (wid == kNTrace + 1) {
+                        for (int a = lane; a < n; a += 32) {
+                            const double jpa = p.obs.jp[a], jma = p.obs.jm[a], mza = p.obs.mz[a];
+                            if (jpa != 0.0) {
+                                const zc r = A::to(rho[(a + 1) * ld + a]);
+                                v0 = fma(jpa, r.x, v0);
+                                v1 = fma(jpa, r.y, v1);
+                            }
+                            if (jma != 0.0) {
+                                const zc r = A::to(rho[(a - 1) * ld + a]);
+                                v2 = fma(jma, r.x, v2);
+                                v3 = fma(jma, r.y, v3);
+                            }
+                            const zc d = A::to(rho[a * ld + a]);
+                            v4 = fma(mza, d.x, v4);
+                            v5 = fma(mza, d.y, v5);
                         }
-                        c0 = fma(mza, d.x, c0);
-                        c1 = fma(mza, d.y, c1);
+                    } else {
+                        for (int e = lane; e < p.obs.n_t1b; e += 32) {
+                            const int ix = p.obs.t1b_idx[e];
+                            const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
+                            v0 = fma(p.obs.t1b_val[e], r.x, v0);
+                            v1 = fma(p.obs.t1b_val[e], r.y, v1);
+                        }
                     }
-                    for (int e = lane; e < p.obs.n_t1b; e += 32) {
-                        const int ix = p.obs.t1b_idx[e];
-                        const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
-                        t0 = fma(p.obs.t1b_val[e], r.x, t0);
-                        t1 = fma(p.obs.t1b_val[e], r.y, t1);
-                    }
-                    const double vals[14] = {z0, z1, n0, n1, t0, t1, p0, p1, m0, m1, c0, c1, j0, j1};
-                    const int slots[14] = {0, 1, 2, 3, 4, 5, 10, 11, 12, 13, 14, 15, 16, 17};
+                    // result slots: z 0,1  n 2,3  t1b 4,5  J+ 10,11  J- 12,13  Jz 14,15  j(j+1) 16,17
+                    const int s0 = wid == 0 ? 0 : (wid == kNTrace + 1 ? 10 : 4);
+                    const int cnt = wid == kNTrace + 2 ? 2 : 6;
+                    const double vals[6] = {v0, v1, v2, v3, v4, v5};
 #pragma unroll
-                    for (int q = 0; q < 14; ++q) {
+                    for (int q = 0; q < 6; ++q) {
+                        if (q >= cnt) break;
                         const double v = warp_sum(vals[q]);
-                        if (lane == 0) fin[slots[q]] = v;
+                        const int slot = (wid == 0 && q >= 4) ? 12 + q : s0 + q;
+                        if (lane == 0) fin[slot] = v;
                     }
                 } else if (p.iE2 && wid <= kNTrace) {  // Q_{2mu} traces: one warp per trace
                     const int q = wid - 1;
