@@ -1302,49 +1302,47 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 }
                 }  // !norm_only
                 __syncthreads();
-                if (threadIdx.x == 0) {
-                    auto get = [&](int slot) {
-                        if (slot >= 6 && slot <= 9) {  // summed over warps
-                            double v = 0.0;
-                            for (int w = 0; w < nw; ++w) v += pw[(slot - 6) * nw + w];
-                            return v;
-                        }
-                        return fin[slot];
-                    };
+                if (wid == 0) {  // accumulation over the gauge points: warp 0, one observable per lane
+                    const unsigned full = 0xffffffffu;
+                    const zc pfv = mk(__shfl_sync(full, pf.x, 0), __shfl_sync(full, pf.y, 0));  // valid in lane 0
+                    double wsum[4];  // energy re/im, <J^2> re/im: per-warp partials summed
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) wsum[q] = warp_sum(lane < nw ? pw[q * nw + lane] : 0.0);
+                    auto get = [&](int slot) { return (slot >= 6 && slot <= 9) ? wsum[slot - 6] : fin[slot]; };
                     const zc zph = mk(p.gphase[2 * (lp * p.nfom + ln)], p.gphase[2 * (lp * p.nfom + ln) + 1]);
-                    const zc norm = onishi ? pf : (p.vacfac * det0 * det1) * (pf * zph);
+                    const zc norm = onishi ? pfv : (p.vacfac * det0 * det1) * (pfv * zph);
                     const zc trp = mk(get(10), get(11)), trm = mk(get(12), get(13)), trz = mk(get(14), get(15));
                     const zc j2 = mk(get(16) + get(8), get(17) + get(9)) + trp * trm + trz * trz;
                     const zc ekin = mk(get(4), get(5));
-                    acc[0] = acc[0] + norm;
                     zc hg = mk(0.0, 0.0);  // H/N at this gauge point (0 when not computed)
                     if (!p.norm_only && !sing) hg = ekin + mk(get(6), get(7)) + mk(p.e0, 0.0);
-                    if (gout) {  // per gauge point: N (with the gauge phase) and H/N
-                        double *g = gout + 4LL * (((long long)pair * p.n_euler + ie) * p.n_gauge + lp * p.nfom + ln);
-                        g[0] = norm.x;
-                        g[1] = norm.y;
-                        g[2] = hg.x;
-                        g[3] = hg.y;
+                    if (lane == 0) {
+                        acc[0] = acc[0] + norm;
+                        if (gout) {  // per gauge point: N (with the gauge phase) and H/N
+                            double *g = gout + 4LL * (((long long)pair * p.n_euler + ie) * p.n_gauge + lp * p.nfom + ln);
+                            g[0] = norm.x;
+                            g[1] = norm.y;
+                            g[2] = hg.x;
+                            g[3] = hg.y;
+                        }
+                        int f = (under == 1) ? 1 : (under == 2 ? 4 : 0);
+                        if (!p.norm_only && sing) f |= 2;
+                        flags |= f;
                     }
-                    int f = (under == 1) ? 1 : (under == 2 ? 4 : 0);
-                    if (p.norm_only) {
-                    } else if (sing) {
-                        f |= 2;
-                    } else {
-                        acc[1] = zfma(norm, mk(get(0), get(1)), acc[1]);
-                        acc[2] = zfma(norm, mk(get(2), get(3)), acc[2]);
-                        acc[3] = zfma(norm, ekin, acc[3]);
-                        acc[6] = zfma(norm, hg, acc[6]);
-                        acc[7] = zfma(norm, j2, acc[7]);
-                        for (int b = 0; b < (r1out ? p.obs.n_r1b : 0); ++b)
+                    if (!p.norm_only && !sing) {
+                        zc o = mk(0.0, 0.0);
+                        bool use = true;
+                        if (lane == 1) o = mk(get(0), get(1));
+                        else if (lane == 2) o = mk(get(2), get(3));
+                        else if (lane == 3) o = ekin;
+                        else if (lane == 6) o = hg;
+                        else if (lane == 7) o = j2;
+                        else if (lane >= 8 && lane < 18 && p.iE2) o = mk(fin[2 * lane + 2], fin[2 * lane + 3]);  // Q slots 18..37
+                        else use = false;
+                        if (use) acc[lane] = zfma(norm, o, acc[lane]);
+                        for (int b = lane; b < (r1out ? p.obs.n_r1b : 0); b += 32)
                             acc_r1b[b] = zfma(norm, mk(red[kR1BSlot + 2 * b], red[kR1BSlot + 2 * b + 1]), acc_r1b[b]);
-                        if (p.iE2)
-                            for (int q = 0; q < 5; ++q) {
-                                acc[8 + q] = zfma(norm, mk(get(18 + 2 * q), get(19 + 2 * q)), acc[8 + q]);
-                                acc[13 + q] = zfma(norm, mk(get(28 + 2 * q), get(29 + 2 * q)), acc[13 + q]);
-                            }
                     }
-                    flags |= f;
                 }
                 __syncthreads();
             }
