@@ -32,6 +32,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -45,17 +47,35 @@ FORM_TEXT = {"fp64": "plain FP64",
 # 20,736-point launch, scaled by points; profiles/point_kernel_fp64_pf.md): all per-point
 # matrices live in shared memory or an L2-resident slot, so traffic is tiny.
 TRAFFIC_BYTES_PER_POINT = 532224.0 / 20736.0
-# Algorithmic FP64 work per kernel point (pf, n = 40, P_G = 81): the minimal flops of
-# the algorithm the kernel runs (a complex multiply-add = 8 flops, complex x real = 4).
-# Per Euler point, amortised over the gauge points: rotation, W-solve and T22 partials,
-# (8+24+16) n^3 / P_G. Per point: the Pfaffian of the n x n Schur complement
-# c (D X D - Z0^-1), (4/3) n^3 (the reference's 2n x 2n form would be (4/3) (2n)^3);
-# Y T22^-1 for the 2n x n right-hand sides as LU + solves, (8/3 + 16) n^3; the three
-# density products complex x real (U0, V0 are real), 12 n^3; the irreducible sparse
-# two-body contraction, 14,442 records x 24 flops. (The generic count of 40 n^3 for the
-# densities and 16 n^3 for the inverse over-counts this algorithm.)
-def algorithmic_flops_per_point(n, n_gauge, nrec):
-    return (48.0 * n ** 3 / n_gauge + (4.0 / 3.0 + 8.0 / 3.0 + 16.0 + 12.0) * n ** 3) + 24.0 * nrec
+
+
+def algorithmic_flops_per_point(wl, n_gauge):
+    """Algorithmic FP64 work per kernel point: the minimal flops of the algorithm the
+    kernel runs (complex multiply-add = 8 flops, complex x real = 4), O(n^2) terms left out.
+
+    Per Euler point, amortised over the n_gauge gauge points: R W, R V1, conj(R) U1 and
+    X = (R W) R^T with the block-diagonal rotation, (3 * 4 + 8) n sum_b d_b^2, and the
+    four T22 partials (n x n x h, complex x real), 8 n^3.
+    Per point: the Pfaffian of the n x n Schur complement c (D X D - Z0^-1), (4/3) n^3;
+    Y T22^-1 for the 2n x n right-hand sides counted as LU + solves, (8/3 + 16) n^3;
+    the density products, 12 n^3. For a species-split pair (charge-conserving vacua:
+    no proton-neutron blocks) these run on two h x h blocks, h = n/2: a quarter.
+    Two-body records: 52 flops (28 when i + j = k + l, which halves the terms); for a
+    split pair the proton-neutron records keep two of the four density products, 18 (10).
+    """
+    n = wl.sp.nlev
+    h = n // 2
+    sd2 = sum(d * d for _, d in wl.sp.blocks())
+    split = all(not np.any(np.asarray(M)[:h, h:]) and not np.any(np.asarray(M)[h:, :h])
+                for U, V in wl.vacua for M in (U, V))
+    r = np.asarray(wl.recs)
+    i, j, k, l = r.T
+    pn = (i < h) & (j >= h) & (k < h) & (l >= h) if split else np.zeros(len(r), bool)
+    diag = (i + j) == (k + l)
+    rec = (52.0 * np.sum(~pn & ~diag) + 28.0 * np.sum(~pn & diag)
+           + 18.0 * np.sum(pn & ~diag) + 10.0 * np.sum(pn & diag))
+    dense = (4.0 / 3.0 + 8.0 / 3.0 + 16.0 + 12.0) * n ** 3 * (0.25 if split else 1.0)
+    return (20.0 * n * sd2 + 8.0 * n ** 3) / n_gauge + dense + float(rec)
 
 
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -453,7 +473,7 @@ def main():
     # ---- rooflines of the dominant kernel (the point kernel; setup is < 0.1 %). The FP64
     # form is bound by the FP64 pipe; the double-float form does the same algorithmic
     # work on the FP32 pipes, so its FP64-equivalent rate may exceed the FP64 peak.
-    flops_pt = algorithmic_flops_per_point(wl.sp.nlev, G, len(wl.recs))
+    flops_pt = algorithmic_flops_per_point(wl, G)
     pts_launch = pps * pts_per_pair
     peak = fp64_peak_tflops(torch) if rank == 0 else None
     ach_form = flops_pt * pts_launch / (statistics.mean(kern_ms) / 1e3) / 1e12
