@@ -189,6 +189,47 @@ int pnamp_batch_rho1b(pnamp_ctx *ctx, int npairs, const double *uv, double *zres
  * rho1b ([nblocks][P_E] complex). PNAMP_ERR_SMALL_NORM when |N^0| <= 1e-8. */
 int pnamp_project_rho1b(const pnamp_ctx *ctx, const double *zres, const double *rho1b, double *out);
 
+/* ---- Two-body transition density of the projected ground state (Rho2B) ---
+ * Replaces ZRho2B_Angles / ZRho2B_Integral and the valence entries of Write_ME2B
+ * (PNAMP_Rho2B.f90:6-296, called from PNAMP_Kernel3D.f90:369,379,722 when
+ * Input%idens != 0), over the two-particle blocks of ME2B_Base_Full
+ * (PNAMP_ME2B_Base.f90:112-205) built on the model space's orbits:
+ *   Rho2BN(bm, a_ij, a_kl) = sum_{m} <j_i m_i j_j m_j|J M> <j_k m_k j_l m_l|J M> / (2J + 1)
+ *       x <q| c+_i c+_j c_l c_k P^{J=0} P^N P^Z |q'> / <q| P^{J=0} P^N P^Z |q'>.
+ * Orbits are numbered in order of first appearance of (n, l, 2j) in the model
+ * space (protons first); tt = 0 nn, 1 np, 2 pp; PP = 0 positive parity.
+ *
+ * pnamp_rho2b_layout needs no device: sizes[5] = {blocks, states, elements
+ * (sum over blocks of states^2), quadruples, terms}. pnamp_rho2b_tables fills
+ * (each may be NULL) blocks [nblocks][4] = (tt, PP, J, states), states
+ * [nstates][2] = (o1, o2), quads [nquads] = levels k_i | k_j << 8 | k_k << 16 |
+ * k_l << 24 (0-based, the tnljm order), elem_ptr [nelements + 1] and, per term,
+ * term_q (quadruple) and term_c (cg1 cg2 / (2J + 1)). PNAMP_ERR_UNSUPPORTED when
+ * an orbit exists for one species only. */
+int pnamp_rho2b_layout(const pnamp_space *sp, int *sizes);
+int pnamp_rho2b_tables(const pnamp_space *sp, int *blocks, int *states, unsigned int *quads, int *elem_ptr,
+                       int *term_q, double *term_c);
+
+/* pnamp_batch_device that also writes, per pair and quadruple (k_i, k_j, k_k, k_l),
+ * sum_e w_e (1/N_FOM^2) sum_phi N(Omega_e, phi) [rho_ki rho_lj - rho_li rho_kj +
+ * kappa01_ij kappa10_kl] into d_rho2b [npairs][nquads] complex (overwritten). Each
+ * CTA keeps its sums in FP64 in device memory the context owns ([grid][nquads]
+ * complex) and adds them into d_rho2b once per Euler point. PNAMP_ERR_STATE in
+ * norm-only mode. */
+int pnamp_batch_rho2b_device(pnamp_ctx *ctx, int npairs, const double *d_uv, double *d_zres,
+                             int *d_point_status, double *d_rho2b, void *stream);
+
+/* The same with host buffers (uv, zres, point_status as pnamp_batch; rho2b
+ * [npairs][nquads] complex). */
+int pnamp_batch_rho2b(pnamp_ctx *ctx, int npairs, const double *uv, double *zres,
+                      int *point_status, double *rho2b);
+
+/* One pair's Rho2BN per element (bm, a_ij, a_kl) in block order, out[nelements]
+ * complex, from its zres (ZRES(P_E, NOBS) column-major) and rho2b ([nquads]
+ * complex); Write_ME2B prints the real parts. PNAMP_ERR_SMALL_NORM when
+ * |N^0| <= 1e-8. */
+int pnamp_project_rho2b(pnamp_ctx *ctx, const double *zres, const double *rho2b, double *out);
+
 /* Same computation as pnamp_batch_device, for callers that must not allocate
  * device memory per call: code running under a runtime that owns the device
  * memory budget (a caching allocator or an MPS client with a hard memory cap),

@@ -294,15 +294,127 @@ def rho1b_write_me1b(table, zres, r, mesh: Mesh):
     return np.array([np.real(zr[b] / zn) / math.sqrt(key[4] + 1.0) for b, (key, _) in enumerate(table)])
 
 
+def rho2b_blocks(sp: ModelSpace):
+    """Two-particle blocks |(nlj)_1 (nlj)_2; J, PP, tt> of ME2B_Base_Full
+    (PNAMP_ME2B_Base.f90:112-205) over the model space's orbits.
+
+    Returns [(tt, PP, J, [(o1, o2), ...])] in the block order bm of
+    PNAMP_ME2B_Base.f90:182-205 (tt = 0 nn, 1 np, 2 pp; PP = 0 positive parity;
+    J ascending); o1, o2 index `sp.orbits`. Within a block the states follow the
+    enumeration of PNAMP_ME2B_Base.f90:128-171: (l1, j1), (l2, j2) ascending by
+    LJ = (2l + 2j - 1)/2, then n1, n2; for nn and pp only id1 <= id2
+    (id = n + nMax LJ) and identical orbits only at even J. The reference builds
+    the blocks over its full oscillator space; restricted to the model space the
+    numbering is the reference's whenever the model space is that full space.
+    """
+    nmax = max(n0 for n0, _, _ in sp.orbits) + 1
+    lj = lambda o: (2 * sp.orbits[o][1] + sp.orbits[o][2] - 1) // 2
+    ident = lambda o: sp.orbits[o][0] + 1 + nmax * lj(o)
+    orbs = sorted(range(len(sp.orbits)), key=lambda o: (lj(o), sp.orbits[o][0]))
+    ljs = sorted({lj(o) for o in orbs})
+    blocks = {}
+    for tt in range(3):
+        for lj1 in ljs:
+            for lj2 in ljs:
+                o1s = [o for o in orbs if lj(o) == lj1]
+                o2s = [o for o in orbs if lj(o) == lj2]
+                _, l1, tj1 = sp.orbits[o1s[0]]
+                _, l2, tj2 = sp.orbits[o2s[0]]
+                pp = (l1 + l2) % 2
+                for J in range(abs(tj1 - tj2) // 2, (tj1 + tj2) // 2 + 1):
+                    for o1 in o1s:
+                        for o2 in o2s:
+                            if tt != 1 and ident(o1) > ident(o2):
+                                continue
+                            if J % 2 == 1 and o1 == o2 and tt != 1:
+                                continue
+                            blocks.setdefault((tt, pp, J), []).append((o1, o2))
+    return [(tt, pp, J, blocks[(tt, pp, J)]) for (tt, pp, J) in sorted(blocks)]
+
+
+def _level(sp: ModelSpace, o, t_ref, tm):
+    """tnljm%level(m, lj, n, t) for the reference's t (1 proton, 0 neutron)."""
+    t = -1 if t_ref == 1 else 1
+    for k in range(sp.nlev):
+        if sp.t[k] == t and sp.orbit[k] == o and sp.twom[k] == tm:
+            return k
+    raise KeyError((o, t_ref, tm))
+
+
+def rho2b_terms(sp: ModelSpace, blocks=None):
+    """The m sums of ZRho2B_Angles (PNAMP_Rho2B.f90:31-118) as a sparse map.
+
+    Returns (quads [nq, 4] of levels (k_i, k_j, k_k, k_l), terms) where terms lists,
+    per element (bm, a_ij, a_kl) in block order, [(q, cg1 cg2 / (2J + 1)), ...].
+    Every quadruple conserves M = m_i + m_j = m_k + m_l; quads are unique and in
+    first-use order."""
+    from sccm_gb300.basis import cg
+    blocks = rho2b_blocks(sp) if blocks is None else blocks
+    qidx, quads, terms = {}, [], []
+    for tt, _pp, J, states in blocks:
+        t1, t2 = tt // 2, (tt + 1) // 2
+        for oi, oj in states:
+            tji, tjj = sp.orbits[oi][2], sp.orbits[oj][2]
+            for ok, ol in states:
+                tjk, tjl = sp.orbits[ok][2], sp.orbits[ol][2]
+                el = []
+                for mi in range(-tji, tji + 1, 2):
+                    ki = _level(sp, oi, t1, mi)
+                    for mj in range(-tjj, tjj + 1, 2):
+                        kj = _level(sp, oj, t2, mj)
+                        c1 = cg(tji, tjj, 2 * J, mi, mj, mi + mj)
+                        for mk in range(-tjk, tjk + 1, 2):
+                            ml = mi + mj - mk
+                            if abs(ml) > tjl:
+                                continue
+                            c2 = cg(tjk, tjl, 2 * J, mk, ml, mi + mj)
+                            if c1 * c2 == 0.0:
+                                continue
+                            key = (ki, kj, _level(sp, ok, t1, mk), _level(sp, ol, t2, ml))
+                            if key not in qidx:
+                                qidx[key] = len(quads)
+                                quads.append(key)
+                            el.append((qidx[key], c1 * c2 / (2 * J + 1)))
+                terms.append(el)
+    return np.array(quads, dtype=np.int64).reshape(-1, 4), terms
+
+
+def rho2b_point(quads, rho, k10, k01, znorm):
+    """One gauge point of ZRho2B_Angles before the CG sums (PNAMP_Rho2B.f90:105-112):
+    znorm [ZRO(k,i) ZRO(l,j) - ZRO(l,i) ZRO(k,j) + ZKAPA01(i,j) ZKAPA10(k,l)] per quadruple
+    (the 1/NFOM^2 is applied with the gauge mean)."""
+    i, j, k, l = quads.T
+    return znorm * (rho[k, i] * rho[l, j] - rho[l, i] * rho[k, j] + k01[i, j] * k10[k, l])
+
+
+def rho2b_write_me2b(terms, zres, a, mesh: Mesh):
+    """ZRho2B_Integral at J = 0 and the valence entries of Write_ME2B
+    (PNAMP_Rho2B.f90:137-296) for one pair.
+
+    a [P_E, nq] are the gauge means from `kernel_triaxial(..., rho2b=quads)`. Returns
+    the complex Rho2BN per element (bm, a_ij, a_kl) in block order, = sum_e w_e
+    sum_q c_q a_eq / N^0 (the J = 0 weight cancels in the ratio), or None when
+    |N^0| <= CHOP (Rho2BN = 0 there in the reference)."""
+    w = mesh.euler_points()[:, 3]
+    zn = np.sum(w * zres[:, 0])
+    if abs(zn) <= CHOP:
+        return None
+    za = w @ a
+    return np.array([sum(c * za[q] for q, c in el) for el in terms], complex) / zn
+
+
 def kernel_triaxial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1,
-                    cscale=1.0, iscale=0, iE2=True, euler_subset=None, point_log=None, rho1b=None):
+                    cscale=1.0, iscale=0, iE2=True, euler_subset=None, point_log=None, rho1b=None,
+                    rho2b=None):
     """Kernel4Triaxial mesh loop (PNAMP_Kernel3D.f90:70-407) -> ZRES[P_E, NOBS].
 
     Shell-model runs take the Pfaffian branch (ide forced to 1, Kernel3D.f90:140-159)
     unless NFOM = 1, where the Onishi formula gives the norm (Kernel3D.f90:286-290). `euler_subset` restricts the loop to a list of Euler
     indices (rows of ZRES left zero elsewhere) so tests can sample large meshes.
     With `rho1b` (a `rho1b_table`), returns (ZRES, R) with R[P_E, nblocks] the
-    gauge means of ZRho1B_Angles (Kernel3D.f90:367).
+    gauge means of ZRho1B_Angles (Kernel3D.f90:367). With `rho2b` (the quads of
+    `rho2b_terms`), returns (ZRES, A) with A[P_E, nq] the gauge means of
+    `rho2b_point` (ZRho2B_Angles, Kernel3D.f90:369); both: (ZRES, R, A).
     """
     n = sp.nlev
     U0, V0, U1, V1 = (np.asarray(x, dtype=float) for x in (U0, V0, U1, V1))
@@ -317,6 +429,7 @@ def kernel_triaxial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1
     nf = mesh.nfom
     zres = np.zeros((len(pts), NOBS), complex)
     r1 = np.zeros((len(pts), len(rho1b) if rho1b is not None else 0), complex)
+    r2 = np.zeros((len(pts), len(rho2b) if rho2b is not None else 0), complex)
     idx = range(len(pts)) if euler_subset is None else euler_subset
     for ie in idx:
         alp, bet, gam, _w = pts[ie]
@@ -339,9 +452,13 @@ def kernel_triaxial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1
                 acc += o
                 if rho1b is not None:
                     r1[ie] += rho1b_point(rho1b, rokappa(A, U0, V0, U1, V1)[0], znorm)
+                if rho2b is not None:
+                    r2[ie] += rho2b_point(rho2b, *rokappa(A, U0, V0, U1, V1), znorm)
         zres[ie] = acc / nf ** 2
         r1[ie] /= nf ** 2
-    return (zres, r1) if rho1b is not None else zres
+        r2[ie] /= nf ** 2
+    out = (zres,) + ((r1,) if rho1b is not None else ()) + ((r2,) if rho2b is not None else ())
+    return out if len(out) > 1 else zres
 
 
 def kernel_axial(sp: ModelSpace, ham: Hamiltonian, mesh: Mesh, U0, V0, U1, V1, iE2=True):

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -46,6 +47,15 @@ struct pnamp_ctx {
     std::vector<double> euler_w;
     double *d_r1b = nullptr;
     long long r1b_cap = 0;
+    // two-body density tables (built on first use) and device buffers
+    std::vector<int> sp_t, sp_n, sp_l, sp_tj, sp_tm;
+    bool r2_built = false;
+    std::vector<int> r2_blocks, r2_states, r2_ptr, r2_tq;
+    std::vector<uint32_t> r2_quads;
+    std::vector<double> r2_tc;
+    uint32_t *d_r2q = nullptr;
+    double *d_r2acc = nullptr, *d_r2out = nullptr;
+    long long r2acc_cap = 0, r2out_cap = 0;
 };
 
 namespace {
@@ -193,6 +203,113 @@ int ensure_batch(pnamp_ctx *c, int npairs) {
     return PNAMP_OK;
 }
 
+
+// Two-body density tables: the blocks of ME2B_Base_Full (PNAMP_ME2B_Base.f90:112-205)
+// over the model space's orbits and the m sums of ZRho2B_Angles (PNAMP_Rho2B.f90:31-118).
+struct R2Tables {
+    std::vector<int> blocks;        // [nblocks][4]: tt (0 nn, 1 np, 2 pp), PP, J, number of states
+    std::vector<int> states;        // [nstates][2]: orbits o1, o2 (first-appearance order of (n, l, j))
+    std::vector<uint32_t> quads;    // packed k_i | k_j << 8 | k_k << 16 | k_l << 24, first-use order
+    std::vector<int> ptr, tq;       // per element (bm, a_ij, a_kl): terms [ptr[e], ptr[e+1])
+    std::vector<double> tc;         // cg1 cg2 / (2J + 1) of each term
+};
+
+int build_r2(int n, const int *t, const int *nn1, const int *l, const int *tj, const int *tm, R2Tables &r) {
+    // orbits (n, l, 2j) in order of first appearance (protons first, .val order)
+    std::vector<std::array<int, 3>> orb;
+    std::vector<int> lev_orb(n);
+    for (int k = 0; k < n; ++k) {
+        const std::array<int, 3> key{nn1[k], l[k], tj[k]};
+        int o = (int)(std::find(orb.begin(), orb.end(), key) - orb.begin());
+        if (o == (int)orb.size()) orb.push_back(key);
+        lev_orb[k] = o;
+    }
+    const int no = (int)orb.size();
+    // level of (reference t: 1 proton / 0 neutron, orbit, 2m)
+    std::vector<int> lev((size_t)2 * no * 16, -1);
+    for (int k = 0; k < n; ++k) {
+        if (tj[k] > 15 || std::abs(tm[k]) > tj[k]) return PNAMP_ERR_ARG;
+        const int tr = (t[k] == -1) ? 1 : 0;
+        lev[((size_t)tr * no + lev_orb[k]) * 16 + (tm[k] + tj[k]) / 2] = k;
+    }
+    auto level = [&](int tr, int o, int m2) { return lev[((size_t)tr * no + o) * 16 + (m2 + orb[o][2]) / 2]; };
+    for (int o = 0; o < no; ++o)
+        for (int tr = 0; tr < 2; ++tr)
+            for (int m2 = -orb[o][2]; m2 <= orb[o][2]; m2 += 2)
+                if (level(tr, o, m2) < 0) return PNAMP_ERR_UNSUPPORTED;  // orbit of one species only
+    int nmax = 0;
+    for (const auto &q : orb) nmax = std::max(nmax, q[0]);
+    auto lj = [&](int o) { return (2 * orb[o][1] + orb[o][2] - 1) / 2; };
+    auto ident = [&](int o) { return orb[o][0] + nmax * lj(o); };
+    std::vector<int> sorted(no);
+    for (int o = 0; o < no; ++o) sorted[o] = o;
+    std::stable_sort(sorted.begin(), sorted.end(), [&](int a, int b) {
+        return lj(a) != lj(b) ? lj(a) < lj(b) : orb[a][0] < orb[b][0];
+    });
+    std::vector<int> ljs;
+    for (int o : sorted)
+        if (ljs.empty() || ljs.back() != lj(o)) ljs.push_back(lj(o));
+    // enumeration of PNAMP_ME2B_Base.f90:128-171 grouped by block (tt, PP, J)
+    std::map<std::array<int, 3>, std::vector<std::array<int, 2>>> blk;
+    for (int tt = 0; tt < 3; ++tt)
+        for (int lj1 : ljs)
+            for (int lj2 : ljs) {
+                std::vector<int> o1s, o2s;
+                for (int o : sorted) {
+                    if (lj(o) == lj1) o1s.push_back(o);
+                    if (lj(o) == lj2) o2s.push_back(o);
+                }
+                const int l1 = orb[o1s[0]][1], tj1 = orb[o1s[0]][2], l2 = orb[o2s[0]][1], tj2 = orb[o2s[0]][2];
+                const int pp = (l1 + l2) % 2;
+                for (int J = std::abs(tj1 - tj2) / 2; J <= (tj1 + tj2) / 2; ++J)
+                    for (int o1 : o1s)
+                        for (int o2 : o2s) {
+                            if (tt != 1 && ident(o1) > ident(o2)) continue;
+                            if (J % 2 == 1 && o1 == o2 && tt != 1) continue;
+                            blk[{tt, pp, J}].push_back({o1, o2});
+                        }
+            }
+    std::map<uint32_t, int> qidx;
+    r.ptr.assign(1, 0);
+    for (const auto &kv : blk) {
+        const int tt = kv.first[0], J = kv.first[2];
+        const int t1 = tt / 2, t2 = (tt + 1) / 2;
+        const auto &st = kv.second;
+        r.blocks.insert(r.blocks.end(), {tt, kv.first[1], J, (int)st.size()});
+        for (const auto &a : st) r.states.insert(r.states.end(), {a[0], a[1]});
+        for (const auto &ij : st)
+            for (const auto &kl : st) {
+                const int tji = orb[ij[0]][2], tjj = orb[ij[1]][2], tjk = orb[kl[0]][2], tjl = orb[kl[1]][2];
+                for (int mi = -tji; mi <= tji; mi += 2)
+                    for (int mj = -tjj; mj <= tjj; mj += 2) {
+                        const double c1 = cg_h(tji, tjj, 2 * J, mi, mj, mi + mj);
+                        for (int mk = -tjk; mk <= tjk; mk += 2) {
+                            const int ml = mi + mj - mk;
+                            if (std::abs(ml) > tjl) continue;
+                            const double c2 = cg_h(tjk, tjl, 2 * J, mk, ml, mi + mj);
+                            if (c1 * c2 == 0.0) continue;
+                            const uint32_t key = (uint32_t)level(t1, ij[0], mi) | ((uint32_t)level(t2, ij[1], mj) << 8) |
+                                                 ((uint32_t)level(t1, kl[0], mk) << 16) |
+                                                 ((uint32_t)level(t2, kl[1], ml) << 24);
+                            auto it = qidx.find(key);
+                            int q;
+                            if (it == qidx.end()) {
+                                q = (int)r.quads.size();
+                                qidx.emplace(key, q);
+                                r.quads.push_back(key);
+                            } else {
+                                q = it->second;
+                            }
+                            r.tq.push_back(q);
+                            r.tc.push_back(c1 * c2 / (2 * J + 1));
+                        }
+                    }
+                r.ptr.push_back((int)r.tq.size());
+            }
+    }
+    return PNAMP_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -233,6 +350,8 @@ void pnamp_free(pnamp_ctx *ctx) {
     if (!ctx) return;
     for (void *q : ctx->allocs) cudaFree(q);
     if (ctx->d_r1b) cudaFree(ctx->d_r1b);
+    for (void *q : {(void *)ctx->d_r2q, (void *)ctx->d_r2acc, (void *)ctx->d_r2out})
+        if (q) cudaFree(q);
     for (void *q : {(void *)ctx->d_pairbuf, (void *)ctx->d_scratch, (void *)ctx->d_uv, (void *)ctx->d_zres,
                     (void *)ctx->d_status, (void *)ctx->d_proj, (void *)ctx->d_projq})
         if (q) cudaFree(q);
@@ -468,6 +587,11 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
             UP(val, ot.r1b_val);
         }
         for (size_t e = 3; e < euler.size(); e += 4) c->euler_w.push_back(euler[e]);
+        c->sp_t.assign(sp->t, sp->t + n);
+        c->sp_n.assign(sp->n, sp->n + n);
+        c->sp_l.assign(sp->l, sp->l + n);
+        c->sp_tj.assign(sp->twoj, sp->twoj + n);
+        c->sp_tm.assign(sp->twom, sp->twom + n);
     }
 #undef UP
     p.obs = ot;
@@ -497,6 +621,9 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
     }
     p.form = 0;
     p.norm_only = 0;
+    p.n_r2q = 0;  // two-body density launches set their own copy
+    p.r2q = nullptr;
+    p.r2acc = nullptr;
     c->grid = std::max(c->grid_form[0], c->grid_form[1]);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         pnamp_free(c);
@@ -640,6 +767,147 @@ int pnamp_project_rho1b(const pnamp_ctx *c, const double *zres, const double *rh
         }
         // AE = Re(sum / N), written divided by sqrt(2j + 1) (PNAMP_Rho1B.f90:82-84)
         out[b] = (sr * nr + si * ni) / d / std::sqrt(c->r1b_twoj[b] + 1.0);
+    }
+    return PNAMP_OK;
+}
+
+int pnamp_rho2b_layout(const pnamp_space *sp, int *sizes) {
+    if (!sp || !sizes || !sp->t || !sp->n || !sp->l || !sp->twoj || !sp->twom) return PNAMP_ERR_ARG;
+    if (sp->nlev < 2 || sp->nlev > PNAMP_MAX_NLEV) return PNAMP_ERR_ARG;
+    R2Tables r;
+    const int rc = build_r2(sp->nlev, sp->t, sp->n, sp->l, sp->twoj, sp->twom, r);
+    if (rc) return rc;
+    sizes[0] = (int)r.blocks.size() / 4;
+    sizes[1] = (int)r.states.size() / 2;
+    sizes[2] = (int)r.ptr.size() - 1;
+    sizes[3] = (int)r.quads.size();
+    sizes[4] = (int)r.tq.size();
+    return PNAMP_OK;
+}
+
+int pnamp_rho2b_tables(const pnamp_space *sp, int *blocks, int *states, unsigned int *quads, int *elem_ptr,
+                       int *term_q, double *term_c) {
+    if (!sp || !sp->t || !sp->n || !sp->l || !sp->twoj || !sp->twom) return PNAMP_ERR_ARG;
+    if (sp->nlev < 2 || sp->nlev > PNAMP_MAX_NLEV) return PNAMP_ERR_ARG;
+    R2Tables r;
+    const int rc = build_r2(sp->nlev, sp->t, sp->n, sp->l, sp->twoj, sp->twom, r);
+    if (rc) return rc;
+    if (blocks) std::copy(r.blocks.begin(), r.blocks.end(), blocks);
+    if (states) std::copy(r.states.begin(), r.states.end(), states);
+    if (quads) std::copy(r.quads.begin(), r.quads.end(), quads);
+    if (elem_ptr) std::copy(r.ptr.begin(), r.ptr.end(), elem_ptr);
+    if (term_q) std::copy(r.tq.begin(), r.tq.end(), term_q);
+    if (term_c) std::copy(r.tc.begin(), r.tc.end(), term_c);
+    return PNAMP_OK;
+}
+
+namespace {
+int ensure_r2(pnamp_ctx *c) {
+    if (!c->r2_built) {
+        R2Tables r;
+        const int n = c->p.n;
+        const int rc = build_r2(n, c->sp_t.data(), c->sp_n.data(), c->sp_l.data(), c->sp_tj.data(),
+                                c->sp_tm.data(), r);
+        if (rc) return rc;
+        if (r.quads.empty()) return PNAMP_ERR_UNSUPPORTED;
+        CK(cudaMalloc(&c->d_r2q, r.quads.size() * sizeof(uint32_t)));
+        CK(cudaMemcpy(c->d_r2q, r.quads.data(), r.quads.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        c->r2_blocks.swap(r.blocks);
+        c->r2_states.swap(r.states);
+        c->r2_quads.swap(r.quads);
+        c->r2_ptr.swap(r.ptr);
+        c->r2_tq.swap(r.tq);
+        c->r2_tc.swap(r.tc);
+        c->r2_built = true;
+    }
+    const long long need = 2LL * (long long)c->r2_quads.size() * c->grid_form[c->p.form];
+    if (need > c->r2acc_cap) {
+        if (c->d_r2acc) cudaFree(c->d_r2acc);
+        c->d_r2acc = nullptr;
+        c->r2acc_cap = 0;
+        CK(cudaMalloc(&c->d_r2acc, (size_t)need * sizeof(double)));
+        c->r2acc_cap = need;
+    }
+    return PNAMP_OK;
+}
+}  // namespace
+
+int pnamp_batch_rho2b_device(pnamp_ctx *c, int npairs, const double *d_uv, double *d_zres, int *d_status,
+                             double *d_rho2b, void *stream) {
+    if (!c || npairs < 0 || (npairs > 0 && (!d_uv || !d_zres || !d_status || !d_rho2b))) return PNAMP_ERR_ARG;
+    if (c->p.norm_only) return PNAMP_ERR_STATE;
+    int rc = ensure_r2(c);
+    if (rc) return rc;
+    if (npairs == 0) return PNAMP_OK;
+    rc = ensure_pairs(c, npairs);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
+    Params q = c->p;
+    q.n_r2q = (int)c->r2_quads.size();
+    q.r2q = c->d_r2q;
+    q.r2acc = c->d_r2acc;
+    CK(cudaMemsetAsync(d_rho2b, 0, (size_t)npairs * q.n_r2q * 2 * sizeof(double), st));
+    CK(launch_setup(q, npairs, d_uv, c->d_pairbuf, st));
+    CK(launch_points(q, npairs, c->d_pairbuf, c->d_scratch, c->grid_form[q.form], d_zres, d_status, st, nullptr, 0,
+                     nullptr, nullptr, d_rho2b));
+    return PNAMP_OK;
+}
+
+int pnamp_batch_rho2b(pnamp_ctx *c, int npairs, const double *uv, double *zres, int *point_status,
+                      double *rho2b) {
+    if (!c || npairs < 0 || (npairs > 0 && (!uv || !zres || !rho2b))) return PNAMP_ERR_ARG;
+    if (npairs == 0) return PNAMP_OK;
+    int rc = ensure_batch(c, npairs);
+    if (rc) return rc;
+    rc = ensure_r2(c);
+    if (rc) return rc;
+    const long long rb = 2LL * npairs * (long long)c->r2_quads.size();
+    if (rb > c->r2out_cap) {
+        if (c->d_r2out) cudaFree(c->d_r2out);
+        c->d_r2out = nullptr;
+        c->r2out_cap = 0;
+        CK(cudaMalloc(&c->d_r2out, (size_t)rb * sizeof(double)));
+        c->r2out_cap = rb;
+    }
+    const long long nn = (long long)c->p.n * c->p.n;
+    const size_t zbytes = (size_t)npairs * 2 * kNobs * c->p.n_euler * sizeof(double);
+    const size_t sbytes = (size_t)npairs * c->p.n_euler * sizeof(int);
+    CK(cudaMemcpyAsync(c->d_uv, uv, (size_t)npairs * 4 * nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    rc = pnamp_batch_rho2b_device(c, npairs, c->d_uv, c->d_zres, c->d_status, c->d_r2out, c->stream);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(zres, c->d_zres, zbytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(rho2b, c->d_r2out, (size_t)rb * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    std::vector<int> st((size_t)npairs * c->p.n_euler);
+    CK(cudaMemcpyAsync(st.data(), c->d_status, sbytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (point_status) memcpy(point_status, st.data(), sbytes);
+    for (int v : st)
+        if (v & PNAMP_ST_SINGULAR_U) return PNAMP_ERR_SINGULAR_U;
+    return PNAMP_OK;
+}
+
+int pnamp_project_rho2b(pnamp_ctx *c, const double *zres, const double *rho2b, double *out) {
+    if (!c || !zres || !rho2b || !out) return PNAMP_ERR_ARG;
+    const int rc = ensure_r2(c);
+    if (rc) return rc;
+    const int P = c->p.n_euler;
+    // N^0 over the Euler weights (the J = 0 weight cancels against ZRho2B_Integral's)
+    double nr = 0.0, ni = 0.0;
+    for (int e = 0; e < P; ++e) {
+        nr += c->euler_w[e] * zres[2 * e];
+        ni += c->euler_w[e] * zres[2 * e + 1];
+    }
+    if (std::sqrt(nr * nr + ni * ni) <= 1e-8) return PNAMP_ERR_SMALL_NORM;  // Rho2BN = 0 in Write_ME2B
+    const double d = nr * nr + ni * ni;
+    const int ne = (int)c->r2_ptr.size() - 1;
+    for (int e = 0; e < ne; ++e) {
+        double sr = 0.0, si = 0.0;
+        for (int t = c->r2_ptr[e]; t < c->r2_ptr[e + 1]; ++t) {
+            sr += c->r2_tc[t] * rho2b[2 * c->r2_tq[t]];
+            si += c->r2_tc[t] * rho2b[2 * c->r2_tq[t] + 1];
+        }
+        out[2 * e] = (sr * nr + si * ni) / d;       // (sr + i si) / (nr + i ni)
+        out[2 * e + 1] = (si * nr - sr * ni) / d;
     }
     return PNAMP_OK;
 }

@@ -92,6 +92,11 @@ struct Params {
     ObsTables obs;
     PairLayout pl;
     Placement place;
+    // two-body density quadruples (ZRho2B_Angles): packed 8-bit k_i, k_j, k_k, k_l, and the
+    // per-CTA FP64 accumulators [grid][n_r2q] complex; n_r2q = 0 outside Rho2B launches
+    int n_r2q;
+    const uint32_t *r2q;
+    double *r2acc;
 };
 
 // Contexts of one multi-context launch, passed by value (kernel parameter space).
@@ -110,7 +115,7 @@ cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *
 cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc *scratch,
                           int grid, double *zres, int *status, cudaStream_t st,
                           const int2 *items = nullptr, long long nitems = 0, double *gout = nullptr,
-                          double *r1out = nullptr);
+                          double *r1out = nullptr, double *r2out = nullptr);
 cudaError_t launch_proj_weights(const Params &p, int axial, zc *w, cudaStream_t st);
 cudaError_t launch_project(const Params &p, int npairs, const zc *w, const double *zres,
                            int core_prot, int core_neut, int chop, double *out, cudaStream_t st);

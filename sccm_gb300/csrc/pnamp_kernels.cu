@@ -774,6 +774,7 @@ cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *
 // ------------------------------------------------------------------ points
 constexpr int kNSlot = 36;  // observable sums: slots 0..37 final values, then per-warp partials
 constexpr int kR1BSlot = 128;  // one-body density block sums: red[kR1BSlot + 2b], re and im
+constexpr int kR2Norm = 260;   // the gauge point's norm, re and im, for the two-body density pass
 static_assert(kThreads >= 32 * (kNTrace + 1), "one warp per Q trace plus warp 0");
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -790,7 +791,8 @@ template <class Z>
 __device__ __forceinline__ void point_item(const Params &p, const double *__restrict__ pairbuf, zc *slot,
                                            int pair, int ie, bool reload, double *__restrict__ zres,
                                            int *__restrict__ status, double *__restrict__ gout = nullptr,
-                                           double *__restrict__ r1out = nullptr) {
+                                           double *__restrict__ r1out = nullptr,
+                                           double *__restrict__ r2out = nullptr) {
     using A = Ar<Z>;
     using R = typename A::R;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -877,6 +879,13 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
         if (threadIdx.x == 0) {
             for (int io = 0; io < kNobs; ++io) acc[io] = mk(0.0, 0.0);
             for (int b = 0; b < (r1out ? p.obs.n_r1b : 0); ++b) acc_r1b[b] = mk(0.0, 0.0);
+        }
+        // two-body density sums of this Euler point: thread t owns quadruples t, t + blockDim, ...
+        // (zeroed, accumulated and flushed by the same thread, so no barrier between the steps)
+        double *r2acc = r2out ? p.r2acc + 2LL * p.n_r2q * blockIdx.x : nullptr;
+        for (int q = threadIdx.x; q < (r2out ? p.n_r2q : 0); q += blockDim.x) {
+            r2acc[2 * q] = 0.0;
+            r2acc[2 * q + 1] = 0.0;
         }
         __syncthreads();
         // ---- R W (or, for the Onishi norm, R U1 and conj(R) V1), R V1, conj(R) U1 (FP64)
@@ -1318,6 +1327,10 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     if (!p.norm_only && !sing) hg = ekin + mk(get(6), get(7)) + mk(p.e0, 0.0);
                     if (lane == 0) {
                         acc[0] = acc[0] + norm;
+                        if (r2out) {
+                            red[kR2Norm] = norm.x;
+                            red[kR2Norm + 1] = norm.y;
+                        }
                         if (gout) {  // per gauge point: N (with the gauge phase) and H/N
                             double *g = gout + 4LL * (((long long)pair * p.n_euler + ie) * p.n_gauge + lp * p.nfom + ln);
                             g[0] = norm.x;
@@ -1345,6 +1358,23 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     }
                 }
                 __syncthreads();
+                if (r2out && !p.norm_only && !sing) {
+                    // ZRho2B_Angles (PNAMP_Rho2B.f90:105-112) before its Clebsch-Gordan sums:
+                    // N [ZRO(k,i) ZRO(l,j) - ZRO(l,i) ZRO(k,j) + ZKAPA01(i,j) ZKAPA10(k,l)] per quadruple,
+                    // summed over the gauge points in FP64; the densities are still in S here
+                    const zc nrm = mk(red[kR2Norm], red[kR2Norm + 1]);
+                    for (int q = threadIdx.x; q < p.n_r2q; q += blockDim.x) {
+                        const uint32_t pk = p.r2q[q];
+                        const int i = pk & 0xff, j = (pk >> 8) & 0xff, k = (pk >> 16) & 0xff, l = pk >> 24;
+                        Z t = rho[k * ld + i] * rho[l * ld + j];
+                        t = zfms(rho[l * ld + i], rho[k * ld + j], t);
+                        t = zfma(k01[i * ld + j], k10[k * ld + l], t);
+                        const zc a = zfma(nrm, A::to(t), mk(r2acc[2 * q], r2acc[2 * q + 1]));
+                        r2acc[2 * q] = a.x;
+                        r2acc[2 * q + 1] = a.y;
+                    }
+                    __syncthreads();  // the next gauge point overwrites the densities
+                }
             }
         }
         if (threadIdx.x == 0) {
@@ -1364,6 +1394,14 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 r1out[2LL * (((long long)pair * p.obs.n_r1b + b) * p.n_euler + ie) + 1] = v.y;
             }
         }
+        if (r2out) {  // Euler weight x gauge mean, added into the pair's sums (ZRho2B_Integral at J = 0)
+            const double wgt = p.euler[4 * ie + 3] / ((double)p.nfom * p.nfom);
+            double *o = r2out + 2LL * p.n_r2q * pair;
+            for (int q = threadIdx.x; q < p.n_r2q; q += blockDim.x) {
+                atomicAdd(o + 2 * q, wgt * r2acc[2 * q]);
+                atomicAdd(o + 2 * q + 1, wgt * r2acc[2 * q + 1]);
+            }
+        }
         __syncthreads();
     }
 }
@@ -1372,7 +1410,8 @@ template <class Z>
 __global__ void __launch_bounds__(kThreads, 1)
 point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scratch,
              double *__restrict__ zres, int *__restrict__ status, const int2 *__restrict__ items,
-             long long nitems, double *__restrict__ gout, double *__restrict__ r1out) {
+             long long nitems, double *__restrict__ gout, double *__restrict__ r1out,
+             double *__restrict__ r2out) {
     // items == nullptr: every (pair, Euler point) of the batch; else the listed (pair, ie)
     zc *slot = scratch + (long long)blockIdx.x * p.place.slot_elems;
     const long long total = items ? nitems : (long long)npairs * p.n_euler;
@@ -1388,7 +1427,7 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
             pair = (int)(item / p.n_euler);
             ie = (int)(item % p.n_euler);
         }
-        point_item<Z>(p, pairbuf, slot, pair, ie, pair != cur_pair, zres, status, gout, r1out);
+        point_item<Z>(p, pairbuf, slot, pair, ie, pair != cur_pair, zres, status, gout, r1out, r2out);
         cur_pair = pair;
     }
 }
@@ -1480,13 +1519,14 @@ cudaError_t set_point_smem(int form, int bytes) {
 
 cudaError_t launch_points(const Params &p, int npairs, const double *pairbuf, zc *scratch, int grid,
                           double *zres, int *status, cudaStream_t st, const int2 *items, long long nitems,
-                          double *gout, double *r1out) {
+                          double *gout, double *r1out, double *r2out) {
+    if (r2out && (p.n_r2q <= 0 || !p.r2q || !p.r2acc)) return cudaErrorInvalidValue;
     if (p.form == 1)
         point_kernel<zd><<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status,
-                                                                    items, nitems, gout, r1out);
+                                                                    items, nitems, gout, r1out, r2out);
     else
         point_kernel<zc><<<grid, kThreads, p.place.smem_bytes, st>>>(p, npairs, pairbuf, scratch, zres, status,
-                                                                    items, nitems, gout, r1out);
+                                                                    items, nitems, gout, r1out, r2out);
     return cudaGetLastError();
 }
 

@@ -12,13 +12,16 @@
     `rho1b`, each pair's J = 0 one-body density goes to `Rho1B_*.dens` as
     Write_ME1B writes it (PNAMP_Kernel3D.f90:719, PNAMP_Rho1B.f90:63-91);
     a pair whose projected norm is below CHOP gets no density file, as there.
+    With `rho2b`, the two-body density goes to `Rho2B_*.dat` as Write_ME2B writes
+    `Rho2B.dat` (PNAMP_Kernel3D.f90:722, PNAMP_Rho2B.f90:175-296), one file per
+    pair instead of one overwritten name; both densities together cost two passes.
 """
 from __future__ import annotations
 
 import json
 import os
 
-from .formats import atomic_write_text, empty_kernels, write_elem_general, write_rho1b_dens
+from .formats import atomic_write_text, empty_kernels, write_elem_general, write_rho1b_dens, write_rho2b_dat
 from .pnamp import PNAMP_ERR_SMALL_NORM, PnampError
 from .pnamp import PnampContext
 
@@ -45,8 +48,12 @@ def rho1b_name(q1, q2):
     return f"Rho1B_{q1:03d}_{q2:03d}.dens"
 
 
+def rho2b_name(q1, q2):
+    return f"Rho2B_{q1:03d}_{q2:03d}.dat"
+
+
 def run_pairs(ctx: PnampContext, vacua, pairs, out_dir, prefix="kern", coords=None, batch=8,
-              manifest="manifest.json", rho1b=False):
+              manifest="manifest.json", rho1b=False, rho2b=False):
     """Compute and write the kernel files of `pairs` ((q1, q2) 1-based into `vacua`)."""
     os.makedirs(out_dir, exist_ok=True)
     mpath = os.path.join(out_dir, manifest)
@@ -61,13 +68,23 @@ def run_pairs(ctx: PnampContext, vacua, pairs, out_dir, prefix="kern", coords=No
         if rho1b:
             zres, status, r1 = ctx.batch_rho1b(quads)
             blocks = ctx.rho1b_blocks()
-        else:
+        if rho2b:
+            zres, status, r2 = ctx.batch_rho2b(quads)
+            blocks2 = ctx.rho2b_tables()["blocks"]
+        if not (rho1b or rho2b):
             zres, status = ctx.batch(quads)
         for k, (q1, q2) in enumerate(chunk):
             if rho1b:
                 try:
                     vals = ctx.project_rho1b(zres[k], r1[k])
                     atomic_write_text(os.path.join(out_dir, rho1b_name(q1, q2)), write_rho1b_dens, blocks, vals)
+                except PnampError as e:
+                    if e.code != PNAMP_ERR_SMALL_NORM:
+                        raise
+            if rho2b:
+                try:
+                    vals2 = ctx.project_rho2b(zres[k], r2[k])
+                    atomic_write_text(os.path.join(out_dir, rho2b_name(q1, q2)), write_rho2b_dat, blocks2, vals2)
                 except PnampError as e:
                     if e.code != PNAMP_ERR_SMALL_NORM:
                         raise

@@ -378,3 +378,46 @@ def read_rho1b_dens(path):
             if len(tok) == 5:
                 out[tuple(int(x) for x in tok[:4])] = float(tok[4])
     return out
+
+
+def write_rho2b_dat(path, blocks, values, chop=CHOP):
+    """Write_ME2B's kernel-density file (PNAMP_Rho2B.f90:175-296), valence entries.
+
+    `blocks` are (tt, PP, J, states) in block order and `values` the Rho2BN of every
+    element (bm, a_ij, a_kl) in that order (complex or real). Layout: the header lines,
+    'bMax=' (i6) with the last block index, one '(2i10)' line bm, aMax - 1 per block, a
+    blank record pair, then per block '# block' (i6) ':' ' aMax=' (i6) and one '(2i10,f20.10)'
+    line b_ij, b_kl, Re(Rho2BN) (indices from 0) per element with |Rho2BN| > CHOP,
+    followed by a blank record pair."""
+    vals = list(values)
+    with open(path, "w") as f:
+        f.write("*** 2b DME from GCM calculation ***\n")
+        f.write("# basis (block, aMax)\n")
+        f.write(f"bMax={len(blocks) - 1:6d}\n")
+        for bm, (_tt, _pp, _j, st) in enumerate(blocks):
+            f.write(f"{bm:10d}{len(st) - 1:10d}\n")
+        f.write("\n\n")
+        e = 0
+        for bm, (_tt, _pp, _j, st) in enumerate(blocks):
+            f.write(f"# block{bm:6d}: aMax={len(st) - 1:6d}\n")
+            for a in range(len(st)):
+                for b in range(len(st)):
+                    v = vals[e]
+                    e += 1
+                    if abs(v) > chop:
+                        f.write(f"{a:10d}{b:10d}{float(np.real(v)):20.10f}\n")
+            f.write("\n\n")
+
+
+def read_rho2b_dat(path):
+    """A Write_ME2B file -> {(bm, b_ij, b_kl): value}."""
+    out, bm = {}, -1
+    with open(path) as f:
+        for ln in f:
+            if ln.startswith("# block"):
+                bm = int(ln.split(":")[0].split()[-1])
+                continue
+            tok = ln.split()
+            if bm >= 0 and len(tok) == 3:
+                out[(bm, int(tok[0]), int(tok[1]))] = float(tok[2])
+    return out

@@ -27,6 +27,7 @@ PNAMP_ERR_CUDA = 2
 PNAMP_ERR_NOMEM = 3
 PNAMP_ERR_SINGULAR_U = 4
 PNAMP_ERR_UNSUPPORTED = 5
+PNAMP_ERR_STATE = 6
 
 ST_PIVOT_UNDERFLOW = 1
 ST_SINGULAR_T22 = 2
@@ -46,7 +47,8 @@ EXPORTS = ("pnamp_init", "pnamp_n_euler", "pnamp_pair", "pnamp_batch", "pnamp_ba
            "pnamp_project_q", "pnamp_project_q_device", "pnamp_multi_create", "pnamp_multi_schedule",
            "pnamp_multi_launch", "pnamp_multi_items", "pnamp_multi_free", "pnamp_multi_placement",
            "pnamp_set_outputs", "pnamp_batch_items_device", "pnamp_rho1b_blocks", "pnamp_batch_rho1b_device",
-           "pnamp_batch_rho1b", "pnamp_project_rho1b")
+           "pnamp_batch_rho1b", "pnamp_project_rho1b", "pnamp_rho2b_layout", "pnamp_rho2b_tables",
+           "pnamp_batch_rho2b_device", "pnamp_batch_rho2b", "pnamp_project_rho2b")
 FORMS = {"fp64": 0, "df64": 1}
 PNAMP_ERR_SCRATCH_LIMIT = 7
 PNAMP_ERR_SMALL_NORM = 8
@@ -106,6 +108,14 @@ def load_library(path: str | None = None):
                                       C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.pnamp_project_rho1b.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.pnamp_batch_items_device.argtypes = [vp, C.c_int, vp, C.c_longlong, vp, vp, vp, vp, vp]
+    lib.pnamp_rho2b_layout.argtypes = [C.POINTER(_Space), C.POINTER(C.c_int)]
+    lib.pnamp_rho2b_tables.argtypes = [C.POINTER(_Space), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_uint), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_double)]
+    lib.pnamp_batch_rho2b_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp]
+    lib.pnamp_batch_rho2b.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                      C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    lib.pnamp_project_rho2b.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.pnamp_pair.argtypes = [vp] + [C.POINTER(C.c_double)] * 5 + [C.POINTER(C.c_int)]
     lib.pnamp_batch.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_int)]
@@ -146,6 +156,38 @@ def _dptr(a):
 class PairResult:
     zres: np.ndarray      # [P_E, NOBS] complex, ZRES(iang, io)
     status: np.ndarray    # [P_E] int bit flags
+
+
+def rho2b_tables(sp: ModelSpace):
+    """Two-particle blocks and m-sum terms of the two-body density (pnamp_rho2b_layout /
+    pnamp_rho2b_tables; host only, no device needed).
+
+    Returns dict: blocks [(tt, PP, J, [(o1, o2), ...])] in Write_ME2B's block order,
+    quads [nq, 4] levels (k_i, k_j, k_k, k_l), ptr [nelem + 1], term_q, term_c."""
+    lib = load_library()
+    keep = [np.ascontiguousarray(np.asarray(a, dtype=np.int32)) for a in (sp.t, sp.n, sp.l, sp.twoj, sp.twom)]
+    space = _Space(sp.nlev, sp.nprot, sp.nneut, sp.core_prot, sp.core_neut, *[_iptr(a) for a in keep])
+    sizes = np.zeros(5, dtype=np.int32)
+    rc = lib.pnamp_rho2b_layout(C.byref(space), _iptr(sizes))
+    if rc != PNAMP_OK:
+        raise PnampError(rc, "pnamp_rho2b_layout")
+    nb, ns, ne, nq, nt = (int(x) for x in sizes)
+    blk = np.zeros((nb, 4), dtype=np.int32)
+    st = np.zeros((ns, 2), dtype=np.int32)
+    quads = np.zeros(nq, dtype=np.uint32)
+    ptr = np.zeros(ne + 1, dtype=np.int32)
+    tq = np.zeros(nt, dtype=np.int32)
+    tc = np.zeros(nt)
+    rc = lib.pnamp_rho2b_tables(C.byref(space), _iptr(blk), _iptr(st),
+                                quads.ctypes.data_as(C.POINTER(C.c_uint)), _iptr(ptr), _iptr(tq), _dptr(tc))
+    if rc != PNAMP_OK:
+        raise PnampError(rc, "pnamp_rho2b_tables")
+    blocks, s0 = [], 0
+    for tt, pp, J, na in blk:
+        blocks.append((int(tt), int(pp), int(J), [tuple(int(x) for x in st[s0 + a]) for a in range(na)]))
+        s0 += na
+    q4 = np.stack([(quads >> (8 * k)) & 0xFF for k in range(4)], axis=1).astype(np.int64)
+    return {"blocks": blocks, "quads": q4, "ptr": ptr, "term_q": tq, "term_c": tc}
 
 
 class PnampContext:
@@ -322,6 +364,40 @@ class PnampContext:
                                                 r.ctypes.data_as(C.POINTER(C.c_double)), _dptr(out))
         if rc != PNAMP_OK:
             raise PnampError(rc, "pnamp_project_rho1b")
+        return out
+
+    def rho2b_tables(self):
+        """The context's two-body density tables (see the module-level `rho2b_tables`)."""
+        if getattr(self, "_r2", None) is None:
+            self._r2 = rho2b_tables(self.sp)
+        return self._r2
+
+    def batch_rho2b(self, pairs_or_packed):
+        """-> (zres [npairs, P_E, NOBS], status, rho2b [npairs, nquads]) through the host-buffer ABI;
+        rho2b = sum_e w_e (gauge mean of N x the quadruple's density product)."""
+        uv = pairs_or_packed if isinstance(pairs_or_packed, np.ndarray) else self.pack_pairs(pairs_or_packed)
+        uv = np.ascontiguousarray(uv, dtype=np.float64)
+        npairs = uv.shape[0]
+        nq = self.rho2b_tables()["quads"].shape[0]
+        z = np.zeros((npairs, NOBS, self.n_euler), dtype=np.complex128)
+        st = np.zeros((npairs, self.n_euler), dtype=np.int32)
+        r = np.zeros((npairs, nq), dtype=np.complex128)
+        rc = load_library().pnamp_batch_rho2b(self._h, npairs, _dptr(uv), z.ctypes.data_as(C.POINTER(C.c_double)),
+                                              _iptr(st), r.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_batch_rho2b")
+        return np.ascontiguousarray(z.transpose(0, 2, 1)), st, r
+
+    def project_rho2b(self, zres, rho2b):
+        """One pair: zres [P_E, NOBS], rho2b [nquads] -> complex Rho2BN per element in block order."""
+        z = np.ascontiguousarray(np.asarray(zres, dtype=np.complex128).T)
+        r = np.ascontiguousarray(np.asarray(rho2b, dtype=np.complex128))
+        out = np.zeros(len(self.rho2b_tables()["ptr"]) - 1, dtype=np.complex128)
+        rc = load_library().pnamp_project_rho2b(self._h, z.ctypes.data_as(C.POINTER(C.c_double)),
+                                                r.ctypes.data_as(C.POINTER(C.c_double)),
+                                                out.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_project_rho2b")
         return out
 
     def set_outputs(self, outputs):
