@@ -286,6 +286,67 @@ def uneven_main(args):
     return 0
 
 
+def rho2b_main(args):
+    """`--workload rho2b`: the pf workload with the two-body transition density on.
+
+    One step = setup + the point kernel with the per-quadruple Rho2B sums
+    (`pnamp_batch_rho2b_device`) over `--pairs-per-step` pairs; beside it the same
+    pairs without densities (`pnamp_batch_device`). Roofline of the Rho2B pass: per
+    point and quadruple one complex product difference, one complex multiply-add
+    and the norm-weighted FP64 accumulation, 30 flops, and a 16-byte read and write
+    of the CTA's accumulator (L2-resident); the kernel is timed whole.
+    """
+    import torch
+    from sccm_gb300.pnamp import PnampContext
+    from sccm_gb300.synth import config
+    from sccm_gb300.uneven import time_launches
+
+    torch.cuda.set_device(0)
+    wl = config(1)
+    pps = args.pairs_per_step
+    ctx = PnampContext(wl.sp, wl.e0, wl.t1b, wl.recs, wl.vbar, wl.mesh, q2=wl.q2, form=args.form)
+    nq = ctx.rho2b_tables()["quads"].shape[0]
+    dev = torch.device("cuda")
+    uv = torch.from_numpy(ctx.pack_pairs([(*wl.vacua[i], *wl.vacua[j]) for i, j in wl.pairs[:pps]])).to(dev)
+    z = torch.zeros((pps, 19, ctx.n_euler, 2), dtype=torch.float64, device=dev)
+    st = torch.zeros((pps, ctx.n_euler), dtype=torch.int32, device=dev)
+    r2 = torch.zeros((pps, nq, 2), dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+
+    def dens():
+        ctx.batch_rho2b_device(pps, uv.data_ptr(), z.data_ptr(), st.data_ptr(), r2.data_ptr(), s)
+
+    def plain():
+        ctx.batch_device(pps, uv.data_ptr(), z.data_ptr(), st.data_ptr(), s)
+
+    for _ in range(args.warmup):
+        dens()
+        plain()
+    torch.cuda.synchronize()
+    with ClockSampler(os.path.join(ROOT, "gpurun_out", "clocks_rho2b.csv")
+                      if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/pnamp_clocks_rho2b.csv") as clk:
+        d_ms, d_all = time_launches(dens, args.steps, flush=flush.zero_)
+    p_ms, _ = time_launches(plain, args.steps, flush=flush.zero_)
+    pts = pps * ctx.n_euler * wl.mesh.n_gauge
+    extra_s = (d_ms - p_ms) / 1e3
+    print(json.dumps({
+        "metric": "projected kernel points/s with the two-body transition density (Rho2B)",
+        "value": pts / (d_ms / 1e3), "unit": "points/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": d_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "df64" if args.form == "df64" else "f64",
+        "data": "synthetic: seeded vacua and TBMEs",
+        "config": {"workload": WORKLOAD, "pairs_per_step": pps, "quadruples": nq, "form": FORM_TEXT[args.form],
+                   "l2": "flushed (256 MiB write) before each step"},
+        "step_ms": d_all, "without_densities": {"value": pts / (p_ms / 1e3), "ms_per_step": p_ms},
+        "rho2b_pass": {"flops_per_point": 30.0 * nq, "extra_ms_per_step": d_ms - p_ms,
+                       "tflops_of_extra_time": 30.0 * nq * pts / extra_s / 1e12 if extra_s > 0 else None,
+                       "accumulator_bytes_per_point": 32.0 * nq},
+        "clocks": clk.summary(0), "gpu_launches": 2}))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -301,9 +362,10 @@ def main():
     ap.add_argument("--no-compare", action="store_true", help="skip timing the plain FP64 form as well")
     ap.add_argument("--mesh", default=None,
                     help="override the mesh as NALP,NBET,NGAM,NFOM (small cases for profiling captures)")
-    ap.add_argument("--workload", default="pf", choices=["pf", "uneven", "learned"],
+    ap.add_argument("--workload", default="pf", choices=["pf", "uneven", "learned", "rho2b"],
                     help="pf: the 210-pair pf-shell set (headline); uneven: three model spaces in one launch; "
-                         "learned: learned + mixed against exact mixed on a fine mesh")
+                         "learned: learned + mixed against exact mixed on a fine mesh; rho2b: the pf set with "
+                         "the two-body transition density")
     ap.add_argument("--learned-vacua", type=int, default=6)
     ap.add_argument("--learned-train", type=int, default=10)
     ap.add_argument("--uneven-scale", type=int, default=1, help="divide the uneven batch's pair counts")
@@ -315,6 +377,8 @@ def main():
         return uneven_main(args)
     if args.workload == "learned":
         return learned_main(args)
+    if args.workload == "rho2b":
+        return rho2b_main(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -424,6 +424,12 @@ class PnampContext:
         if rc != PNAMP_OK:
             raise PnampError(rc, "pnamp_batch_device")
 
+    def batch_rho2b_device(self, npairs, d_uv, d_zres, d_status, d_rho2b, stream=0):
+        rc = load_library().pnamp_batch_rho2b_device(self._h, npairs, C.c_void_p(d_uv), C.c_void_p(d_zres),
+                                                     C.c_void_p(d_status), C.c_void_p(d_rho2b), C.c_void_p(stream))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_batch_rho2b_device")
+
     def project_device(self, npairs, d_zres, d_out, chop=True, stream=0):
         rc = load_library().pnamp_project_device(self._h, npairs, C.c_void_p(d_zres), 1 if chop else 0,
                                                  C.c_void_p(d_out), C.c_void_p(stream))
