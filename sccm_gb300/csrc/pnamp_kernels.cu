@@ -522,102 +522,125 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &u
 // row-major, ld h, the second at S + h*h), eliminated together by the thread group g:
 // each step takes both 2x2 pivots (row pivoting as in pfaffian_upper; warp b of the group
 // searches matrix b), so the species-split form of a point needs h/2 - 1 steps for both
-// species. Returns Pf(first) * Pf(second) in the group's thread 0. `vec` holds 2h scratch
-// values, `flag` 4 ints.
+// species. Two group barriers per step: (a) the exchange of column c with the pivot column
+// and the scaled pivot row v = S[c][.] / S[r][c] in one pass, (b) the rank-2 update, in
+// which warp b first updates the next pivot row of matrix b and searches it (pivot index,
+// value and reciprocal for the next step), then joins the rest of the update. A small pivot
+// (|S[r][c]|^2 <= 1e-26, PNAMP_Proj.f90:290,333) or a non-finite one is recorded and the
+// elimination runs on (its values are discarded): the result is 0 with `underflow` set.
+// Returns Pf(first) * Pf(second) and `underflow` in the group's thread 0. `vec` holds 2h
+// scratch values, `pv` 4 (pivots and reciprocals), `flag` 4 ints.
 template <class Z>
-__device__ zc pfaffian_upper2(const Grp &g, Z *S, int h, Z *vec, int *flag, int &underflow) {
+__device__ zc pfaffian_upper2(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *flag, int &underflow) {
     using A = Ar<Z>;
     const int lane = g.tid & 31, wid = g.wid;
     const int hh = h * h;
+    const int nstep = h / 2 - 1;
     zc pf = mk(1.0, 0.0);
-    underflow = 0;
-    for (int k = 0; k < h / 2 - 1; ++k) {
-        const int r = 2 * k, c = r + 1;
-        if (wid < 2) {  // warp b: pivot of row r of matrix b
-            const Z *Sb = S + wid * hh;
-            unsigned long long best = 0ull;
-            int bidx = 0x7fffffff;
-            for (int j = c + lane; j < h; j += 32) {
-                const unsigned long long key = A::key(Sb[r * h + j]);
-                if (key > best || bidx == 0x7fffffff) {
-                    best = key;
-                    bidx = j;
-                }
+    int uf = 0;
+    // warp b: pivot of row r of matrix b over columns c..h-1 -> flag[b] (index), flag[2 + b]
+    // (0 fine, 1 small, 2 non-finite), pv[b] (value), pv[2 + b] (reciprocal)
+    auto search = [&](int b, int r) {
+        const Z *Sb = S + b * hh;
+        unsigned long long best = 0ull;
+        int bidx = 0x7fffffff;
+        for (int j = r + 1 + lane; j < h; j += 32) {
+            const unsigned long long key = A::key(Sb[r * h + j]);
+            if (key > best || bidx == 0x7fffffff) {
+                best = key;
+                bidx = j;
             }
+        }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const unsigned long long ob = __shfl_down_sync(0xffffffffu, best, o);
-                const int oi = __shfl_down_sync(0xffffffffu, bidx, o);
-                if (oi != 0x7fffffff && (bidx == 0x7fffffff || ob > best || (ob == best && oi < bidx))) {
-                    best = ob;
-                    bidx = oi;
-                }
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long ob = __shfl_down_sync(0xffffffffu, best, o);
+            const int oi = __shfl_down_sync(0xffffffffu, bidx, o);
+            if (oi != 0x7fffffff && (bidx == 0x7fffffff || ob > best || (ob == best && oi < bidx))) {
+                best = ob;
+                bidx = oi;
             }
-            if (lane == 0) flag[2 + wid] = bidx;
         }
-        gsync(g);
-        const int q0 = flag[2], q1 = flag[3];
-        if (q0 == 0x7fffffff || q1 == 0x7fffffff) {
-            underflow = 2;
-            return mk(0.0, 0.0);
+        if (lane == 0) {
+            const int q = (bidx == 0x7fffffff) ? r + 1 : bidx;  // at least one candidate when r + 1 < h
+            const Z ssz = Sb[r * h + q];
+            const zc ss = A::to(ssz);
+            const int f = (bidx == 0x7fffffff || !zfinite(ss)) ? 2 : (!(abs2(ss) > 1.0e-26) ? 1 : 0);
+            flag[b] = q;
+            flag[2 + b] = f;
+            pv[b] = ssz;
+            pv[2 + b] = f ? ssz : zrecip(ssz);
         }
-        // exchange columns/rows c <-> q of each matrix (exch_upper on both at once)
+    };
+    if (nstep > 0 && wid < 2) search(wid, 0);
+    gsync(g);
+    for (int k = 0; k < nstep; ++k) {
+        const int r = 2 * k, c = r + 1;
+        const int q0 = flag[0], q1 = flag[1];
+        if (g.tid == 0) {
+            const int fk = flag[2] > flag[3] ? flag[2] : flag[3];
+            if (uf == 0) uf = fk;  // the first failing step decides, as the early return did
+            for (int b = 0; b < 2; ++b) {
+                const double phas = ((b ? q1 : q0) == c) ? 1.0 : -1.0;
+                pf = phas * (pf * A::to(pv[b]));
+            }
+        }
+        // (a) exchange c <-> q (exch_upper on both matrices) and v_i = S'[c][i] / S'[r][c], i > c
         for (int t = g.tid; t < 2 * (h - r); t += g.nthr) {
             const int b = t / (h - r), i = r + t % (h - r);
             const int q = b ? q1 : q0;
-            if (q == c) continue;
+            const Z inv = pv[2 + b];
             Z *Sb = S + b * hh;
-            const int pp = c;
-            if (i < pp) {
-                const Z x = Sb[i * h + pp];
-                Sb[i * h + pp] = Sb[i * h + q];
+            Z *vb = vec + b * h;
+            if (q == c) {
+                if (i > c) vb[i] = Sb[c * h + i] * inv;
+                continue;
+            }
+            if (i < c) {  // i == r: the pivot moves to column c
+                const Z x = Sb[i * h + c];
+                Sb[i * h + c] = Sb[i * h + q];
                 Sb[i * h + q] = x;
             } else if (i > q) {
-                const Z x = Sb[pp * h + i];
-                Sb[pp * h + i] = Sb[q * h + i];
+                const Z x = Sb[c * h + i];
+                const Z y = Sb[q * h + i];
+                Sb[c * h + i] = y;
                 Sb[q * h + i] = x;
-            } else if (i > pp && i < q) {
-                const Z x = Sb[pp * h + i];
-                Sb[pp * h + i] = -Sb[i * h + q];
+                vb[i] = y * inv;
+            } else if (i > c && i < q) {
+                const Z x = Sb[c * h + i];
+                const Z y = -Sb[i * h + q];
+                Sb[c * h + i] = y;
                 Sb[i * h + q] = -x;
-            } else if (i == pp) {
-                Sb[pp * h + q] = -Sb[pp * h + q];
+                vb[i] = y * inv;
+            } else if (i == c) {  // S'[c][q] = -S[c][q]; its thread also sets v_q
+                const Z y = -Sb[c * h + q];
+                Sb[c * h + q] = y;
+                vb[q] = y * inv;
             }
         }
         gsync(g);
-        if (g.tid == 0) {
-            int f = 0;
-            for (int b = 0; b < 2; ++b) {
-                const Z ssz = S[b * hh + r * h + c];
-                const zc ss = A::to(ssz);
-                const int fb = !zfinite(ss) ? 2 : (!(abs2(ss) > 1.0e-26) ? 1 : 0);
-                if (fb > f) f = fb;
-                if (fb == 0) {
-                    vec[b * h + c] = zrecip(ssz);
-                    const double phas = ((b ? q1 : q0) == c) ? 1.0 : -1.0;
-                    pf = phas * (pf * ss);
-                }
+        // (b) S_ij += v_i S_rj - S_ri v_j for c < i < j; row c + 1 (the next pivot row) first
+        const bool more = k + 1 < nstep;
+        if (wid < 2) {
+            Z *Sb = S + wid * hh;
+            const Z *vb = vec + wid * h;
+            const int i = c + 1;
+            const Z vi = vb[i], sri = Sb[r * h + i];
+            for (int j = i + 1 + lane; j < h; j += 32) {
+                Z sv = Sb[i * h + j];
+                sv = zfma(vi, Sb[r * h + j], sv);
+                sv = zfms(sri, vb[j], sv);
+                Sb[i * h + j] = sv;
             }
-            flag[0] = f;
+            __syncwarp();
+            if (more) search(wid, c + 1);
         }
-        gsync(g);
-        if (flag[0]) {
-            underflow = flag[0];
-            gsync(g);
-            return mk(0.0, 0.0);
-        }
-        for (int t = g.tid; t < 2 * (h - c - 1); t += g.nthr) {
-            const int b = t / (h - c - 1), i = c + 1 + t % (h - c - 1);
-            vec[b * h + i] = S[b * hh + c * h + i] * vec[b * h + c];
-        }
-        gsync(g);
-        const int mm = h - c - 1, TT = mm * (mm - 1) / 2;
+        const int mm = h - c - 2, TT = mm * (mm - 1) / 2;
         for (int t = g.tid; t < 2 * TT; t += g.nthr) {
             const int b = t / TT;
             int i, j;
             tri_index(t - b * TT, mm, i, j);
-            i += c + 1;
-            j += c + 1;
+            i += c + 2;
+            j += c + 2;
             Z *Sb = S + b * hh;
             const Z *vb = vec + b * h;
             Z sv = Sb[i * h + j];
@@ -627,8 +650,11 @@ __device__ zc pfaffian_upper2(const Grp &g, Z *S, int h, Z *vec, int *flag, int 
         }
         gsync(g);
     }
-    if (g.tid == 0) pf = pf * A::to(S[(h - 2) * h + h - 1]) * A::to(S[hh + (h - 2) * h + h - 1]);
-    gsync(g);
+    if (g.tid == 0) {
+        pf = pf * A::to(S[(h - 2) * h + h - 1]) * A::to(S[hh + (h - 2) * h + h - 1]);
+        if (uf) pf = mk(0.0, 0.0);
+    }
+    underflow = uf;
     return pf;
 }
 
@@ -775,6 +801,7 @@ cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *
 constexpr int kNSlot = 36;  // observable sums: slots 0..37 final values, then per-warp partials
 constexpr int kR1BSlot = 128;  // one-body density block sums: red[kR1BSlot + 2b], re and im
 constexpr int kR2Norm = 260;   // the gauge point's norm, re and im, for the two-body density pass
+constexpr int kPfScratch = 608;  // 4 point-arithmetic values (<= 64 B): species Pfaffian pivots
 static_assert(kThreads >= 32 * (kNTrace + 1), "one warp per Q trace plus warp 0");
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -944,16 +971,19 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 // ---- S = Cscale [[D X D, -I], [I, -Z0]] (upper triangle), or for a reduced
                 // pair its Schur complement Cscale (D X D - Z0^-1) (n x n, row stride n)
                 const Z dpp = csz * (zep * zep), dpn = csz * (zep * zen), dnn = csz * (zen * zen);
-                // species split: warps 0-3 build and eliminate the two Schur-complement blocks
-                // while warps 4-15 build T22 and Y and run the Gauss-Jordan solve (named barriers
-                // 1 and 2); both are latency-bound, so running them side by side hides one behind
-                // the other. One CTA barrier joins them before the densities.
+                // species split: warps 0-1 build and eliminate the two Schur-complement blocks
+                // while warps 2-15 build T22 and Y and run the Gauss-Jordan solve (named barriers
+                // 1 and 2); both are latency-bound, so running them side by side hides the
+                // Pfaffians behind the solve, which is the longer of the two (per-group clock
+                // marks: the Pfaffian group of 4 warps finished at 60-76 % of the solve; 2, 3, 4
+                // and 6 Pfaffian warps: 425, 429, 435, 448 ms per pf step). One CTA barrier joins
+                // them before the densities.
                 const bool conc = split && !onishi;
                 int under = 0;
                 zc pf = mk(0.0, 0.0);
                 bool sing = false;
                 if (conc) {
-                    constexpr int kPfWarps = 4;
+                    constexpr int kPfWarps = 2;  // the two pivot searches need one warp each
                     if (wid < kPfWarps) {
                         const Grp g{(int)threadIdx.x, kPfWarps * 32, wid, 1};
                         const int Th = h * (h - 1) / 2;
@@ -967,7 +997,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                             S[b * h * h + i * h + j] = v;
                         }
                         gsync(g);
-                        pf = pfaffian_upper2<Z>(g, S, h, vec, sh, under);
+                        pf = pfaffian_upper2<Z>(g, S, h, vec, reinterpret_cast<Z *>(red + kPfScratch), sh, under);
                         pf = pf * pfz;  // meaningful in thread 0
                     } else if (!p.norm_only) {
                         const Grp g{(int)threadIdx.x - kPfWarps * 32, (int)blockDim.x - kPfWarps * 32,
