@@ -270,7 +270,7 @@ __device__ bool gj_right_solve(T *A, int n, T *Y, int ny, T *prow, T *pinv, int 
 }
 
 // gj_right_solve for two independent systems at once, by the thread group g (at least
-// 3 warps; warps 0 and 1 of the group search the pivots): A holds two h x h matrices
+// 2 warps plus h threads; warps 0 and 1 of the group search the pivots): A holds two h x h matrices
 // (compact, the second at A + h*h) and Y two ny x h blocks (the second at Y + ny*h);
 // Y_b <- Y_b A_b^-1 for b = 0, 1 in h steps of two barriers (warp b searches the pivots
 // of system b). prow holds 2h scratch values, pinv 2, sh 4 ints. Returns true if an
@@ -308,6 +308,8 @@ __device__ bool gj_right_solve2(const Grp &g, T *A, int h, T *Y, int ny, T *prow
         }
     };
     bool sing = false;
+    // phase-2 layout of warps 2..: rpi rows at a time, one column per thread
+    const int rpi = (g.nthr - 64) / h, jc = (g.tid - 64) % h, r0 = (g.tid - 64) / h;
     if (wid < 2) search(wid, 0);
     gsync(g);
     for (int k = 0; k < h; ++k) {
@@ -342,15 +344,16 @@ __device__ bool gj_right_solve2(const Grp &g, T *A, int h, T *Y, int ny, T *prow
                 __syncwarp();
                 search(wid, k + 1);
             }
-        } else {
+        } else if (r0 < rpi && jc != k) {
+            // thread (r0, jc): column jc of every rpi-th row of both systems; the pivot-row
+            // values stay in registers and m_r = row[k] is a broadcast load
             const int nrA = h - k - 2 > 0 ? h - k - 2 : 0;
-            const int per2 = (nrA + ny) * h, stride = g.nthr - 64;
-            for (int t = g.tid - 64; t < 2 * per2; t += stride) {
-                const int b = t >= per2 ? 1 : 0, u = t - b * per2;
-                const int rr = u / h, j = u % h;
-                if (j == k) continue;
+            const int rows_b = nrA + ny;
+            const T pj0 = prow[jc], pj1 = prow[h + jc];
+            for (int R = r0; R < 2 * rows_b; R += rpi) {
+                const int b = R >= rows_b ? 1 : 0, rr = R - b * rows_b;
                 T *row = rr < nrA ? A + b * hh + (k + 2 + rr) * h : Y + b * yh + (rr - nrA) * h;
-                row[j] = sfms(row[k], prow[b * h + j], row[j]);
+                row[jc] = sfms(row[k], b ? pj1 : pj0, row[jc]);
             }
         }
         gsync(g);
