@@ -270,23 +270,16 @@ __device__ bool gj_right_solve(T *A, int n, T *Y, int ny, T *prow, T *pinv, int 
 }
 
 // gj_right_solve for two independent systems at once, by the thread group g (at least
-// 3 warps; warps 0 and 1 of the group search the pivots): A holds two h x h matrices
+// 2 warps plus h threads; warps 0 and 1 of the group search the pivots): A holds two h x h matrices
 // (compact, the second at A + h*h) and Y two ny x h blocks (the second at Y + ny*h);
-// Y_b <- Y_b A_b^-1 for b = 0, 1 in h steps of ONE group barrier each. Step k, with the
-// pivot column c of row k of A_b (row pivoting) and 1/A_b[k][c] from the previous step:
-// every row r > k of A_b and every row of Y_b takes m_r = M[r][c] / A[k][c] into column
-// k, its old column k into column c, and M[r][j] -= m_r P[j] for j != k, P = row k of A_b
-// with columns c and k exchanged (row k itself is finished and read in place). A row is
-// owned by L = ceil(h/2) lanes of one warp (2 columns each), so reading m_r and the old
-// column k before the row is overwritten needs only a warp sync; warp b updates row k + 1
-// of A_b first and searches its pivot for the next step (pivot data double-buffered).
-// pinv holds 4 scratch values, sh 8 ints. Returns true if an exactly zero pivot row was met.
+// Y_b <- Y_b A_b^-1 for b = 0, 1 in h steps of two barriers (warp b searches the pivots
+// of system b). prow holds 2h scratch values, pinv 2, sh 4 ints. Returns true if an
+// exactly zero pivot row was met in either system.
 template <typename T>
-__device__ bool gj_right_solve2(const Grp &g, T *A, int h, T *Y, int ny, T *pinv, int *sh) {
+__device__ bool gj_right_solve2(const Grp &g, T *A, int h, T *Y, int ny, T *prow, T *pinv, int *sh) {
     const int lane = g.tid & 31, wid = g.wid;
     const int hh = h * h, yh = ny * h;
-    // slot s of the pivot data: sh[4s + 2b] column, sh[4s + 2b + 1] zero pivot, pinv[2s + b]
-    auto search = [&](int b, int k, int s) {  // warp b: pivot column of row k of A_b
+    auto search = [&](int b, int k) {  // warp b: pivot column of row k of A_b
         const T *Ab = A + b * hh;
         double v = -1.0;
         int idx = 0x7fffffff;
@@ -309,72 +302,58 @@ __device__ bool gj_right_solve2(const Grp &g, T *A, int h, T *Y, int ny, T *pinv
         if (lane == 0) {
             const bool none = (idx == 0x7fffffff);
             const bool z = none || v == 0.0;
-            sh[4 * s + 2 * b] = none ? k : idx;
-            sh[4 * s + 2 * b + 1] = z ? 1 : 0;
-            pinv[2 * s + b] = z ? szero<T>() : srecip(Ab[k * h + (none ? k : idx)]);
-        }
-    };
-    // one row's update at step k by its L lanes (columns j0, j0 + 1): c pivot column, iv its
-    // reciprocal, P the finished row k of the same system
-    auto update_row = [&](T *row, const T *P, int k, int c, const T &iv, int j0, bool act) {
-        T rc = szero<T>(), rk = szero<T>();
-        if (act) {
-            rc = row[c];
-            rk = row[k];
-        }
-        __syncwarp();
-        if (act) {
-            const T m = smul(rc, iv);
-            for (int j = j0; j < j0 + 2 && j < h; ++j) {
-                if (j == k) {
-                    row[k] = m;
-                } else if (j == c) {
-                    row[c] = sfms(m, P[k], rk);   // the old column k, exchanged into c
-                } else {
-                    row[j] = sfms(m, P[j], row[j]);
-                }
-            }
+            sh[2 * b] = none ? k : idx;
+            sh[2 * b + 1] = z ? 1 : 0;
+            pinv[b] = z ? szero<T>() : srecip(Ab[k * h + (none ? k : idx)]);
         }
     };
     bool sing = false;
-    const int L = (h + 1) / 2, rpw = 32 / L;           // lanes per row, rows per warp
-    const int sub = lane / L, j0 = 2 * (lane % L);     // row within the warp's group, first column
-    const bool lane_ok = sub < rpw;
-    const int nbulk = (g.nthr >> 5) - 2;               // warps 2.. of the group
-    if (wid < 2) search(wid, 0, 0);
+    // phase-2 layout of warps 2..: rpi rows at a time, one column per thread
+    const int rpi = (g.nthr - 64) / h, jc = (g.tid - 64) % h, r0 = (g.tid - 64) / h;
+    if (wid < 2) search(wid, 0);
     gsync(g);
     for (int k = 0; k < h; ++k) {
-        const int s = k & 1;
-        const int c0 = sh[4 * s], c1 = sh[4 * s + 2];
-        if (sh[4 * s + 1] || sh[4 * s + 3]) sing = true;
-        const T pv0 = pinv[2 * s], pv1 = pinv[2 * s + 1];
-        if (wid < 2) {  // warp b: row k + 1 of A_b, then the pivot of the next step
-            if (k + 1 < h) {
-                const int c = wid ? c1 : c0;
-                T *row = A + wid * hh + (k + 1) * h;
-                const T *P = A + wid * hh + k * h;
-                const T rc = row[c], rk = row[k];
-                __syncwarp();
-                const T m = smul(rc, wid ? pv1 : pv0);
-                for (int j = lane; j < h; j += 32) {
-                    if (j == k) row[k] = m;
-                    else if (j == c) row[c] = sfms(m, P[k], rk);
-                    else row[j] = sfms(m, P[j], row[j]);
-                }
-                __syncwarp();
-                search(wid, k + 1, s ^ 1);
+        const int c0 = sh[0], c1 = sh[2];
+        if (sh[1] || sh[3]) sing = true;
+        const T pv0 = pinv[0], pv1 = pinv[1];
+        // phase 1 (both systems): m_r = M[r][c] / A[k][c] into column k, old column k into
+        // column c, the exchanged pivot row into prow
+        const int nrT = h - k - 1, nrows = nrT + ny, per1 = nrows + h;
+        for (int t = g.tid; t < 2 * per1; t += g.nthr) {
+            const int b = t >= per1 ? 1 : 0, u = t - b * per1;
+            const int c = b ? c1 : c0;
+            T *Ab = A + b * hh;
+            if (u < nrows) {
+                T *row = u < nrT ? Ab + (k + 1 + u) * h : Y + b * yh + (u - nrT) * h;
+                const T a = row[c], bb = row[k];
+                row[k] = smul(a, b ? pv1 : pv0);
+                if (c != k) row[c] = bb;
+            } else {
+                const int j = u - nrows;
+                prow[b * h + j] = (j == c) ? Ab[k * h + k] : Ab[k * h + j];
             }
-        } else {
-            // rows k + 2 .. h - 1 of A_b and all rows of Y_b, b = 0, 1: rpw rows per warp pass
+        }
+        gsync(g);
+        // phase 2: M[r][j] -= m_r prow[j] for j != k; warp b takes row k + 1 of A_b, then its pivot
+        if (wid < 2) {
+            if (k + 1 < h) {
+                T *row = A + wid * hh + (k + 1) * h;
+                const T m = row[k];
+                for (int j = lane; j < h; j += 32)
+                    if (j != k) row[j] = sfms(m, prow[wid * h + j], row[j]);
+                __syncwarp();
+                search(wid, k + 1);
+            }
+        } else if (r0 < rpi && jc != k) {
+            // thread (r0, jc): column jc of every rpi-th row of both systems; the pivot-row
+            // values stay in registers and m_r = row[k] is a broadcast load
             const int nrA = h - k - 2 > 0 ? h - k - 2 : 0;
             const int rows_b = nrA + ny;
-            for (int R0 = (wid - 2) * rpw; R0 < 2 * rows_b; R0 += nbulk * rpw) {
-                const int R = R0 + sub;
-                const bool act = lane_ok && R < 2 * rows_b;
-                const int b = (act && R >= rows_b) ? 1 : 0, rr = R - b * rows_b;
-                T *row = !act ? A : (rr < nrA ? A + b * hh + (k + 2 + rr) * h : Y + b * yh + (rr - nrA) * h);
-                update_row(row, A + b * hh + k * h, k, b ? c1 : c0, b ? pv1 : pv0, j0, act);
-                __syncwarp();
+            const T pj0 = prow[jc], pj1 = prow[h + jc];
+            for (int R = r0; R < 2 * rows_b; R += rpi) {
+                const int b = R >= rows_b ? 1 : 0, rr = R - b * rows_b;
+                T *row = rr < nrA ? A + b * hh + (k + 2 + rr) * h : Y + b * yh + (rr - nrA) * h;
+                row[jc] = sfms(row[k], b ? pj1 : pj0, row[jc]);
             }
         }
         gsync(g);
@@ -826,7 +805,6 @@ constexpr int kNSlot = 36;  // observable sums: slots 0..37 final values, then p
 constexpr int kR1BSlot = 128;  // one-body density block sums: red[kR1BSlot + 2b], re and im
 constexpr int kR2Norm = 260;   // the gauge point's norm, re and im, for the two-body density pass
 constexpr int kPfScratch = 608;  // 4 point-arithmetic values (<= 64 B): species Pfaffian pivots
-constexpr int kGjScratch = 616;  // 8 ints: species Gauss-Jordan pivot columns, double-buffered
 static_assert(kThreads >= 32 * (kNTrace + 1), "one warp per Q trace plus warp 0");
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -1042,8 +1020,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                             Y[t] = B[grow * n + b * h + j];
                         }
                         gsync(g);
-                        const bool sg = gj_right_solve2<Z>(g, T, h, Y, 2 * h, vec + 2 * h,
-                                                           reinterpret_cast<int *>(red + kGjScratch));
+                        const bool sg = gj_right_solve2<Z>(g, T, h, Y, 2 * h, invd, vec + 2 * h, sh + 4);
                         if (g.tid == 0) sh[4] = sg ? 1 : 0;
                     }
                     __syncthreads();
@@ -1121,7 +1098,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     if (!conc) {  // (Onishi norm) the whole CTA solves after the norm
                         __syncthreads();
                         const Grp gall{(int)threadIdx.x, (int)blockDim.x, wid, 0};
-                        sing = gj_right_solve2<Z>(gall, T, h, Y, 2 * h, vec, reinterpret_cast<int *>(red + kGjScratch));
+                        sing = gj_right_solve2<Z>(gall, T, h, Y, 2 * h, invd, vec, sh);
                     }
                     // densities of each species block in one pass (rho, kappa10 and kappa01 of an
                     // entry share the loads of Y and V0^T), and zeros across the species
