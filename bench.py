@@ -46,7 +46,7 @@ FORM_TEXT = {"fp64": "plain FP64",
 # DRAM bytes per kernel point of the FP64 point kernel (ncu dram__bytes_read + write on a
 # 20,736-point launch, scaled by points; profiles/point_kernel_fp64_pf.md): all per-point
 # matrices live in shared memory or an L2-resident slot, so traffic is tiny.
-TRAFFIC_BYTES_PER_POINT = (523776.0 + 2304.0) / 20736.0
+TRAFFIC_BYTES_PER_POINT = (553984.0 + 2560.0) / 20736.0
 
 
 def algorithmic_flops_per_point(wl, n_gauge):
