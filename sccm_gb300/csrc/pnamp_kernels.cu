@@ -978,9 +978,9 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 // while warps 2-15 build T22 and Y and run the Gauss-Jordan solve (named barriers
                 // 1 and 2); both are latency-bound, so running them side by side hides the
                 // Pfaffians behind the solve, which is the longer of the two (per-group clock
-                // marks: the Pfaffian group of 4 warps finished at 60-76 % of the solve; 2, 3, 4
-                // and 6 Pfaffian warps: 425, 429, 435, 448 ms per pf step). One CTA barrier joins
-                // them before the densities.
+                // marks: the Pfaffian group of 4 warps finished at 60-76 % of the solve; with the
+                // two-barrier Pfaffian 2, 3 and 4 Pfaffian warps time within 0.4 % of each other,
+                // so the solve keeps 14). One CTA barrier joins them before the densities.
                 const bool conc = split && !onishi;
                 int under = 0;
                 zc pf = mk(0.0, 0.0);
