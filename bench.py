@@ -19,6 +19,11 @@ outside its events.  `e2e`: the same steps through the host-buffer C ABI
 (`pnamp_batch` + `pnamp_project`) from pinned host memory, results read back.
 `--impl reference`: the CPU oracle port (the reference Fortran cannot be
 compiled here), all host cores, bounded samples of the same workload.
+
+Other workloads (their own JSON lines, not the headline): `--workload uneven`
+(three model spaces and meshes in persistent launches and one CUDA graph),
+`--workload learned` (the learned mode against the exact mixed form on a fine
+mesh), `--workload rho2b` (the pf set with the two-body transition density).
 """
 from __future__ import annotations
 
