@@ -224,6 +224,15 @@ int pnamp_batch_rho2b_device(pnamp_ctx *ctx, int npairs, const double *d_uv, dou
 int pnamp_batch_rho2b(pnamp_ctx *ctx, int npairs, const double *uv, double *zres,
                       int *point_status, double *rho2b);
 
+/* Both densities from one pass over the mesh: pnamp_batch_rho1b_device and
+ * pnamp_batch_rho2b_device in one launch (either output may be NULL, not both). */
+int pnamp_batch_densities_device(pnamp_ctx *ctx, int npairs, const double *d_uv, double *d_zres,
+                                 int *d_point_status, double *d_rho1b, double *d_rho2b, void *stream);
+
+/* The same with host buffers (layouts as pnamp_batch_rho1b and pnamp_batch_rho2b). */
+int pnamp_batch_densities(pnamp_ctx *ctx, int npairs, const double *uv, double *zres,
+                          int *point_status, double *rho1b, double *rho2b);
+
 /* One pair's Rho2BN per element (bm, a_ij, a_kl) in block order, out[nelements]
  * complex, from its zres (ZRES(P_E, NOBS) column-major) and rho2b ([nquads]
  * complex); Write_ME2B prints the real parts. PNAMP_ERR_SMALL_NORM when

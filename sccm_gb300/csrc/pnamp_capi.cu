@@ -886,6 +886,78 @@ int pnamp_batch_rho2b(pnamp_ctx *c, int npairs, const double *uv, double *zres, 
     return PNAMP_OK;
 }
 
+int pnamp_batch_densities_device(pnamp_ctx *c, int npairs, const double *d_uv, double *d_zres, int *d_status,
+                                 double *d_rho1b, double *d_rho2b, void *stream) {
+    if (!c || npairs < 0 || (!d_rho1b && !d_rho2b)) return PNAMP_ERR_ARG;
+    if (npairs > 0 && (!d_uv || !d_zres || !d_status)) return PNAMP_ERR_ARG;
+    if (d_rho1b && c->p.obs.n_r1b == 0) return PNAMP_ERR_UNSUPPORTED;
+    if (c->p.norm_only) return PNAMP_ERR_STATE;
+    int rc = d_rho2b ? ensure_r2(c) : PNAMP_OK;
+    if (rc) return rc;
+    if (npairs == 0) return PNAMP_OK;
+    rc = ensure_pairs(c, npairs);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
+    Params q = c->p;
+    if (d_rho2b) {
+        q.n_r2q = (int)c->r2_quads.size();
+        q.r2q = c->d_r2q;
+        q.r2acc = c->d_r2acc;
+        CK(cudaMemsetAsync(d_rho2b, 0, (size_t)npairs * q.n_r2q * 2 * sizeof(double), st));
+    }
+    CK(launch_setup(q, npairs, d_uv, c->d_pairbuf, st));
+    CK(launch_points(q, npairs, c->d_pairbuf, c->d_scratch, c->grid_form[q.form], d_zres, d_status, st, nullptr, 0,
+                     nullptr, d_rho1b, d_rho2b));
+    return PNAMP_OK;
+}
+
+int pnamp_batch_densities(pnamp_ctx *c, int npairs, const double *uv, double *zres, int *point_status,
+                          double *rho1b, double *rho2b) {
+    if (!c || npairs < 0 || (!rho1b && !rho2b) || (npairs > 0 && (!uv || !zres))) return PNAMP_ERR_ARG;
+    if (rho1b && c->p.obs.n_r1b == 0) return PNAMP_ERR_UNSUPPORTED;
+    if (npairs == 0) return PNAMP_OK;
+    int rc = ensure_batch(c, npairs);
+    if (rc) return rc;
+    const long long r1 = rho1b ? (long long)npairs * c->p.obs.n_r1b * c->p.n_euler * 2 : 0;
+    if (r1 > c->r1b_cap) {
+        if (c->d_r1b) cudaFree(c->d_r1b);
+        c->d_r1b = nullptr;
+        c->r1b_cap = 0;
+        CK(cudaMalloc(&c->d_r1b, (size_t)r1 * sizeof(double)));
+        c->r1b_cap = r1;
+    }
+    long long r2 = 0;
+    if (rho2b) {
+        rc = ensure_r2(c);
+        if (rc) return rc;
+        r2 = 2LL * npairs * (long long)c->r2_quads.size();
+        if (r2 > c->r2out_cap) {
+            if (c->d_r2out) cudaFree(c->d_r2out);
+            c->d_r2out = nullptr;
+            c->r2out_cap = 0;
+            CK(cudaMalloc(&c->d_r2out, (size_t)r2 * sizeof(double)));
+            c->r2out_cap = r2;
+        }
+    }
+    const long long nn = (long long)c->p.n * c->p.n;
+    const size_t zbytes = (size_t)npairs * 2 * kNobs * c->p.n_euler * sizeof(double);
+    const size_t sbytes = (size_t)npairs * c->p.n_euler * sizeof(int);
+    CK(cudaMemcpyAsync(c->d_uv, uv, (size_t)npairs * 4 * nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    rc = pnamp_batch_densities_device(c, npairs, c->d_uv, c->d_zres, c->d_status, rho1b ? c->d_r1b : nullptr,
+                                      rho2b ? c->d_r2out : nullptr, c->stream);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(zres, c->d_zres, zbytes, cudaMemcpyDeviceToHost, c->stream));
+    if (rho1b) CK(cudaMemcpyAsync(rho1b, c->d_r1b, (size_t)r1 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    if (rho2b) CK(cudaMemcpyAsync(rho2b, c->d_r2out, (size_t)r2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    std::vector<int> stv((size_t)npairs * c->p.n_euler);
+    CK(cudaMemcpyAsync(stv.data(), c->d_status, sbytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (point_status) memcpy(point_status, stv.data(), sbytes);
+    for (int v : stv)
+        if (v & PNAMP_ST_SINGULAR_U) return PNAMP_ERR_SINGULAR_U;
+    return PNAMP_OK;
+}
+
 int pnamp_project_rho2b(pnamp_ctx *c, const double *zres, const double *rho2b, double *out) {
     if (!c || !zres || !rho2b || !out) return PNAMP_ERR_ARG;
     const int rc = ensure_r2(c);

@@ -14,7 +14,7 @@
     a pair whose projected norm is below CHOP gets no density file, as there.
     With `rho2b`, the two-body density goes to `Rho2B_*.dat` as Write_ME2B writes
     `Rho2B.dat` (PNAMP_Kernel3D.f90:722, PNAMP_Rho2B.f90:175-296), one file per
-    pair instead of one overwritten name; both densities together cost two passes.
+    pair instead of one overwritten name; both densities come from one pass.
 """
 from __future__ import annotations
 
@@ -65,14 +65,18 @@ def run_pairs(ctx: PnampContext, vacua, pairs, out_dir, prefix="kern", coords=No
     for s in range(0, len(todo), batch):
         chunk = todo[s:s + batch]
         quads = [(*vacua[q1 - 1], *vacua[q2 - 1]) for (q1, q2) in chunk]
-        if rho1b:
+        if rho1b and rho2b:
+            zres, status, r1, r2 = ctx.batch_densities(quads)
+        elif rho1b:
             zres, status, r1 = ctx.batch_rho1b(quads)
+        elif rho2b:
+            zres, status, r2 = ctx.batch_rho2b(quads)
+        else:
+            zres, status = ctx.batch(quads)
+        if rho1b:
             blocks = ctx.rho1b_blocks()
         if rho2b:
-            zres, status, r2 = ctx.batch_rho2b(quads)
             blocks2 = ctx.rho2b_tables()["blocks"]
-        if not (rho1b or rho2b):
-            zres, status = ctx.batch(quads)
         for k, (q1, q2) in enumerate(chunk):
             if rho1b:
                 try:

@@ -48,7 +48,8 @@ EXPORTS = ("pnamp_init", "pnamp_n_euler", "pnamp_pair", "pnamp_batch", "pnamp_ba
            "pnamp_multi_launch", "pnamp_multi_items", "pnamp_multi_free", "pnamp_multi_placement",
            "pnamp_set_outputs", "pnamp_batch_items_device", "pnamp_rho1b_blocks", "pnamp_batch_rho1b_device",
            "pnamp_batch_rho1b", "pnamp_project_rho1b", "pnamp_rho2b_layout", "pnamp_rho2b_tables",
-           "pnamp_batch_rho2b_device", "pnamp_batch_rho2b", "pnamp_project_rho2b")
+           "pnamp_batch_rho2b_device", "pnamp_batch_rho2b", "pnamp_project_rho2b",
+           "pnamp_batch_densities_device", "pnamp_batch_densities")
 FORMS = {"fp64": 0, "df64": 1}
 PNAMP_ERR_SCRATCH_LIMIT = 7
 PNAMP_ERR_SMALL_NORM = 8
@@ -116,6 +117,9 @@ def load_library(path: str | None = None):
     lib.pnamp_batch_rho2b.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                       C.POINTER(C.c_int), C.POINTER(C.c_double)]
     lib.pnamp_project_rho2b.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    lib.pnamp_batch_densities_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp]
+    lib.pnamp_batch_densities.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                          C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     lib.pnamp_pair.argtypes = [vp] + [C.POINTER(C.c_double)] * 5 + [C.POINTER(C.c_int)]
     lib.pnamp_batch.argtypes = [vp, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                 C.POINTER(C.c_int)]
@@ -387,6 +391,24 @@ class PnampContext:
         if rc != PNAMP_OK:
             raise PnampError(rc, "pnamp_batch_rho2b")
         return np.ascontiguousarray(z.transpose(0, 2, 1)), st, r
+
+    def batch_densities(self, pairs_or_packed):
+        """-> (zres, status, rho1b [npairs, nblocks, P_E], rho2b [npairs, nquads]) from one pass."""
+        uv = pairs_or_packed if isinstance(pairs_or_packed, np.ndarray) else self.pack_pairs(pairs_or_packed)
+        uv = np.ascontiguousarray(uv, dtype=np.float64)
+        npairs = uv.shape[0]
+        nb = len(self.rho1b_blocks())
+        nq = self.rho2b_tables()["quads"].shape[0]
+        z = np.zeros((npairs, NOBS, self.n_euler), dtype=np.complex128)
+        st = np.zeros((npairs, self.n_euler), dtype=np.int32)
+        r1 = np.zeros((npairs, nb, self.n_euler), dtype=np.complex128)
+        r2 = np.zeros((npairs, nq), dtype=np.complex128)
+        rc = load_library().pnamp_batch_densities(self._h, npairs, _dptr(uv), z.ctypes.data_as(C.POINTER(C.c_double)),
+                                                  _iptr(st), r1.ctypes.data_as(C.POINTER(C.c_double)),
+                                                  r2.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_batch_densities")
+        return np.ascontiguousarray(z.transpose(0, 2, 1)), st, r1, r2
 
     def project_rho2b(self, zres, rho2b):
         """One pair: zres [P_E, NOBS], rho2b [nquads] -> complex Rho2BN per element in block order."""

@@ -114,3 +114,22 @@ def test_driver_writes_rho2b_files(tmp_path):
                     assert abs(got[(bm, a, b)] - vals[e].real) <= 5e-11
                 e += 1
     assert len(got) > 0
+
+
+def test_both_densities_in_one_pass(tmp_path):
+    """pnamp_batch_densities: the one- and two-body densities from one launch equal the
+    separate launches', and the driver writes both files from it."""
+    from sccm_gb300.driver import rank_pairs, rho1b_name, rho2b_name, run_pairs
+    from sccm_gb300.formats import read_rho1b_dens, read_rho2b_dat
+    w = make_workload("sd", 2, Mesh(1, 2, 2, 3), seed=66)
+    pairs = [(*w.vacua[0], *w.vacua[1]), (*w.vacua[1], *w.vacua[1])]
+    with ctx_for(w, "df64") as ctx:
+        z, st, r1, r2 = ctx.batch_densities(pairs)
+        z1, st1, r1s = ctx.batch_rho1b(pairs)
+        z2, st2, r2s = ctx.batch_rho2b(pairs)
+        run_pairs(ctx, w.vacua, rank_pairs([(1, 2)], 0, 1), str(tmp_path), batch=1, rho1b=True, rho2b=True)
+    assert np.array_equal(z, z1) and np.array_equal(z, z2) and np.array_equal(st, st1)
+    assert np.array_equal(r1, r1s)
+    assert np.abs(r2 - r2s).max() <= 1e-13 * np.abs(r2s).max()   # atomic adds: order may differ
+    assert len(read_rho1b_dens(tmp_path / rho1b_name(1, 2))) > 0
+    assert len(read_rho2b_dat(tmp_path / rho2b_name(1, 2))) > 0
