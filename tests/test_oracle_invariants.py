@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from sccm_gb300.basis import JJMAX, Mesh, ModelSpace, SHELLS
+from sccm_gb300.basis import JJMAX, Mesh
 from sccm_gb300.synth import make_workload
 from oracle.pnamp_oracle import (Hamiltonian, gauge_matrix, kernel_triaxial, onishi, pfaf_over,
                                  project, rotation_mat, uvphiomega, zbareover, zpfaffian)
