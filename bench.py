@@ -48,8 +48,8 @@ FORM_TEXT = {"fp64": "plain FP64",
              "df64": "mixed: per-point algebra in double-float (FP32 pairs) on the FP32 pipes, FP64 "
                      "preparation and reductions; norm kernel within 1e-10 of FP64"}
 # DRAM bytes per kernel point of the FP64 point kernel (ncu dram__bytes_read + write on a
-# 20,736-point launch, scaled by points; profiles/point_kernel_fp64_pf.md): all per-point
-# matrices live in shared memory or an L2-resident slot, so traffic is tiny.
+# 20,736-point launch of this workload, scaled by points): all per-point matrices live in
+# shared memory or an L2-resident slot, so traffic is tiny.
 TRAFFIC_BYTES_PER_POINT = (553984.0 + 2560.0) / 20736.0
 
 
@@ -116,6 +116,14 @@ def make_pool(ncores):
 
 
 # ------------------------------------------------------------------ clocks
+def clock_path(args, tag):
+    """nvidia-smi samples of one timed region: `--clock-dir` (default: the system temp dir)."""
+    import tempfile
+    d = args.clock_dir or tempfile.gettempdir()
+    os.makedirs(d, exist_ok=True)
+    return os.path.join(d, f"pnamp_clocks_{tag}_{os.getpid()}.csv")
+
+
 class ClockSampler:
     def __init__(self, path):
         self.path = path
@@ -258,8 +266,7 @@ def uneven_main(args):
     for _ in range(max(0, args.warmup - 1)):
         ub.replay()
     torch.cuda.synchronize()
-    with ClockSampler(os.path.join(ROOT, "gpurun_out", "clocks_uneven.csv")
-                      if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/pnamp_clocks_uneven.csv") as clk:
+    with ClockSampler(clock_path(args, "uneven")) as clk:
         g_ms, g_all = time_launches(ub.replay, args.steps, flush=flush.zero_)
     st = [s.cpu().numpy() for s in ub.status]
     if any((x & ~1).any() for x in st):
@@ -328,8 +335,7 @@ def rho2b_main(args):
         dens()
         plain()
     torch.cuda.synchronize()
-    with ClockSampler(os.path.join(ROOT, "gpurun_out", "clocks_rho2b.csv")
-                      if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/pnamp_clocks_rho2b.csv") as clk:
+    with ClockSampler(clock_path(args, "rho2b")) as clk:
         d_ms, d_all = time_launches(dens, args.steps, flush=flush.zero_)
     p_ms, _ = time_launches(plain, args.steps, flush=flush.zero_)
     pts = pps * ctx.n_euler * wl.mesh.n_gauge
@@ -376,6 +382,8 @@ def main():
     ap.add_argument("--tune-scale", type=int, default=16,
                     help="the autotuner times schedules on the uneven batch divided by this")
     ap.add_argument("--no-tune-cache", action="store_true")
+    ap.add_argument("--clock-dir", default=None,
+                    help="directory for the nvidia-smi clock samples of the timed regions (default: temp dir)")
     args = ap.parse_args()
     if args.workload == "uneven":
         return uneven_main(args)
@@ -482,9 +490,7 @@ def main():
             if dist:
                 dist.barrier()
             evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-            with ClockSampler(os.path.join(ROOT, "gpurun_out", f"clocks_{form}_rank{rank}.csv")
-                              if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                              else f"/tmp/pnamp_clocks_{form}_{rank}.csv") as clk:
+            with ClockSampler(clock_path(args, f"{form}_rank{rank}")) as clk:
                 torch.cuda.synchronize()
                 for k in range(args.steps):
                     flush.zero_()

@@ -97,12 +97,18 @@ def zpfaffian(SK, epsln=1.0e-13):
 
     Skew-symmetric Pfaffian by 2x2-block elimination with a global argmax pivot
     over the remaining upper triangle, scanned row by row (first maximum wins),
-    sign `phas` per exchange, and Pf = 0 as soon as |pivot| <= epsln. The matrix
-    is kept in full skew form; row+column exchanges are pure moves, so the upper
-    triangle matches the reference's upper-triangle storage value for value.
+    sign `phas` per exchange, and Pf = 0 as soon as |pivot| <= epsln. The
+    reference reads and exchanges only the upper triangle (ZExch moves upper
+    entries with sign flips, PNAMP_Proj.f90:356-392), i.e. it takes the Pfaffian
+    of the skew matrix that the upper triangle defines; the input's lower
+    triangle (which for a computed M1 = conj(Vbar) conj(Ubar)^-1 is skew only to
+    rounding) never enters. Here that matrix is formed once, triu - triu^T, and
+    kept in full skew form, so row+column exchanges are pure moves and match the
+    reference's upper-triangle storage value for value.
     Returns (Pf, status) with status 1 when the epsln early exit fired.
     """
-    A = np.array(SK, dtype=complex, copy=True)
+    A = np.triu(np.asarray(SK, dtype=complex), 1)
+    A = A - A.T
     N = A.shape[0]
     if N % 2:
         return 0.0 + 0.0j, 0

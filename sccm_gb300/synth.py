@@ -9,8 +9,14 @@ shapes, sizes and value distributions of the benchmark configurations:
     deformed single-particle Hamiltonian with parameters (beta2, gamma), the
     occupations come from BCS with a seeded gap, and O = exp(0.3 G) is a random
     real rotation whose generator G commutes with time reversal and conserves
-    parity and charge. Time-reversal pairs (k, Tk) carry the pairing, so the
-    vacua are time-reversal symmetric and U is invertible (needed by zbareover).
+    parity and, unless `pn_mix` is set, charge. Time-reversal pairs (k, Tk)
+    carry the pairing, so the vacua are time-reversal symmetric and U is
+    invertible (needed by zbareover). With `pn_mix` the generator has proton-
+    neutron entries too (a random Hermitian generator with only time reversal
+    and parity imposed, as the sd benchmark case is specified), so U and V mix
+    the species like the reference's own HFB vacua with proton-neutron pairing
+    (data/Ti/Ti48_*.wf) and every pair takes the general, not the species-split,
+    path of the kernels.
   * interaction: J-coupled, isospin-symmetric V_JT(ab, cd) ~ N(0, 1 MeV),
     hermitian, parity conserving, uncoupled to the antisymmetrised m-scheme
     list with the Clebsch-Gordan sum of Codes/GCM/HFBA_Hamiltonian.f90:295-365;
@@ -40,21 +46,22 @@ def time_reversal(sp: ModelSpace):
     return tau
 
 
-def _conserving_mask(sp: ModelSpace):
+def _conserving_mask(sp: ModelSpace, charge=True):
     same_t = sp.t[:, None] == sp.t[None, :]
     same_par = (sp.l[:, None] - sp.l[None, :]) % 2 == 0
-    return same_t & same_par
+    return (same_t & same_par) if charge else same_par
 
 
-def random_rotation(sp: ModelSpace, rng, scale=0.3):
-    """O = exp(scale * G): G real antisymmetric, commuting with tau, parity/charge conserving."""
+def random_rotation(sp: ModelSpace, rng, scale=0.3, charge=True):
+    """O = exp(scale * G): G real antisymmetric, commuting with tau, parity conserving
+    and, with `charge`, charge conserving."""
     from scipy.linalg import expm
     n = sp.nlev
     tau = time_reversal(sp)
     g = rng.standard_normal((n, n)) / math.sqrt(n)
     g = g - g.T
     g = 0.5 * (g - tau @ g @ tau)          # tau^-1 = -tau: commutes with tau
-    g *= _conserving_mask(sp)
+    g *= _conserving_mask(sp, charge)
     return expm(scale * g)
 
 
@@ -95,8 +102,9 @@ def bcs_occupations(eps, nval, gap):
 
 
 def deformed_vacuum(sp: ModelSpace, spe_orbit, beta2, gamma_deg, rng, gap=None, rot_scale=0.3,
-                    chi=2.0, q2=None):
-    """Real species-diagonal (U, V) of a deformed BCS vacuum, then a random T-even rotation."""
+                    chi=2.0, q2=None, pn_mix=False):
+    """Real (U, V) of a deformed BCS vacuum (species-diagonal), then a random T-even
+    rotation, which mixes protons and neutrons when `pn_mix` is set."""
     n = sp.nlev
     q2 = q2_operators(sp) if q2 is None else q2
     g = math.radians(gamma_deg)
@@ -123,7 +131,7 @@ def deformed_vacuum(sp: ModelSpace, spe_orbit, beta2, gamma_deg, rng, gap=None, 
         U[np.ix_(idx, idx)] = D @ ub
         V[np.ix_(idx, idx)] = D @ vb
     if rot_scale:
-        O = random_rotation(sp, rng, rot_scale)
+        O = random_rotation(sp, rng, rot_scale, charge=not pn_mix)
         U, V = O @ U, O @ V
     return U, V
 
@@ -233,8 +241,9 @@ SHELL_NUCLEONS = {"sd": (2, 2), "pf": (4, 4), "sdpf": (4, 4)}
 
 
 def make_workload(shell, nvac, mesh: Mesh, seed, name=None, rot_scale=0.3, deformed=True,
-                  nprot=None, nneut=None):
-    """A seeded set of `nvac` vacua on one shell with all symmetric pairs i <= j."""
+                  nprot=None, nneut=None, pn_mix=False):
+    """A seeded set of `nvac` vacua on one shell with all symmetric pairs i <= j
+    (`pn_mix`: vacua that mix protons and neutrons, see the module docstring)."""
     rng = np.random.default_rng(seed)
     z, nn = SHELL_NUCLEONS.get(shell, (2, 2))
     sp = ModelSpace(SHELLS[shell], nprot if nprot is not None else z, nneut if nneut is not None else nn)
@@ -248,20 +257,62 @@ def make_workload(shell, nvac, mesh: Mesh, seed, name=None, rot_scale=0.3, defor
     for k in range(nvac):
         b2 = rng.uniform(0.0, 0.5) if deformed else rng.uniform(0.0, 0.3)
         gd = rng.uniform(0.0, 60.0)
-        vacua.append(deformed_vacuum(sp, spe, b2, gd, rng, rot_scale=rot_scale, q2=q2))
+        vacua.append(deformed_vacuum(sp, spe, b2, gd, rng, rot_scale=rot_scale, q2=q2, pn_mix=pn_mix))
         deform.append((b2, gd))
     pairs = [(i, j) for i in range(nvac) for j in range(i, nvac)]
     return Workload(name or shell, sp, mesh, 0.0, t1b, recs, vbar, q2, vacua, deform, pairs)
 
 
-def config(idx, small=False):
-    """Benchmark configurations (mesh sizes as quoted; `small` shrinks the vacuum count)."""
+def config(idx, small=False, pn_mix=None):
+    """Benchmark configurations (mesh sizes as quoted; `small` shrinks the vacuum count).
+
+    The sd case (0) is specified as random vacua with only time reversal and parity
+    imposed, so its vacua mix protons and neutrons; the pf cases (1, 2) default to
+    charge-conserving deformed vacua (the species-split path) and take `pn_mix=True`
+    for the general path.
+    """
     if idx == 0:
-        return make_workload("sd", 2, Mesh(8, 16, 8, 7), seed=1000, name="sd-2vac-8x16x8-g7", deformed=False)
+        return make_workload("sd", 2, Mesh(8, 16, 8, 7), seed=1000, name="sd-2vac-8x16x8-g7", deformed=False,
+                             pn_mix=True if pn_mix is None else pn_mix)
     if idx in (1, 2):
+        mix = bool(pn_mix)
         return make_workload("pf", 4 if small else 20, Mesh(10, 20, 10, 9), seed=2000,
-                             name="pf-20vac-10x20x10-g9")
+                             name="pf-20vac-10x20x10-g9" + ("-pnmix" if mix else ""), pn_mix=mix)
     raise ValueError(f"unknown configuration {idx}")
+
+
+def workload_from_arrays(name, orbits, nprot, nneut, e0, spe, vbar, U, V, mesh: Mesh, core=(0, 0), deform=None):
+    """A workload from real inputs: a model space (orbit list), E0 and single-particle
+    energies keyed as `formats.read_me1b` returns them, the m-scheme V list in the
+    record order of `formats.mscheme_pairs`, and vacua U[k], V[k] (as `formats.read_wf`
+    returns them)."""
+    from .formats import onebody_matrix
+    sp = ModelSpace([tuple(int(x) for x in o) for o in orbits], int(nprot), int(nneut), int(core[0]), int(core[1]))
+    recs = mscheme_pairs(sp)
+    vbar = np.asarray(vbar, dtype=np.float64)
+    if vbar.shape != (len(recs),):
+        raise ValueError(f"{len(vbar)} m-scheme values for {len(recs)} records")
+    vacua = [(np.asarray(U[k], dtype=np.float64), np.asarray(V[k], dtype=np.float64)) for k in range(len(U))]
+    pairs = [(i, j) for i in range(len(vacua)) for j in range(i, len(vacua))]
+    return Workload(name, sp, mesh, float(e0), onebody_matrix(sp, spe), recs, vbar, q2_operators(sp), vacua,
+                    list(deform) if deform is not None else [(0.0, 0.0)] * len(vacua), pairs)
+
+
+def ti48_workload(mesh: Mesh, path=None):
+    """The reference's own Ti48 / KB3G inputs (pf shell, Z = 2, N = 6 valence, eight HFB
+    vacua beta2 = -0.3 ... 0.4 with proton-neutron pairing) from the committed fixture
+    `tests/golden/reference_pins.npz` (built from the SCCM tree by
+    tests/golden/make_reference_pins.py)."""
+    import os
+    if path is None:
+        path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                            "tests", "golden", "reference_pins.npz")
+    d = np.load(path)
+    spe = {tuple(int(x) for x in k): float(v) for k, v in zip(d["kb3g_spe_keys"], d["kb3g_spe_vals"])}
+    betas = [float(b) for b in d["ti48_betas"]]
+    return workload_from_arrays("ti48-kb3g", d["pf_orbits"], d["ti48_nprot"], d["ti48_nneut"], d["kb3g_e0"], spe,
+                                d["kb3g_vbar"], d["ti48_U"], d["ti48_V"], mesh, core=(20, 20),
+                                deform=[(b, 0.0) for b in betas])
 
 
 def uneven_workloads(scale=1):

@@ -1,8 +1,11 @@
 """Build tests/golden/ge76_fixture.npz from the reference's shipped Ge76 data.
 
-Run once in a checkout that has the SCCM reference tree (default path below,
-override with SCCM_REF). The fixture carries everything the Ge76 parity tests
-need, so the tests never read the reference tree at run time:
+Run once with SCCM_REF set to the root of a jmyao17/SCCM checkout:
+
+    SCCM_REF=/path/to/SCCM python tests/golden/make_ge76_fixture.py
+
+The fixture carries everything the Ge76 parity tests need, so the tests never
+read the reference tree at run time:
 
   * the pf5g9 valence space (Codes/val/pf5g9.val)
   * E0 and single-particle energies (Codes/int/GCN2850/SM_GCN2850_ME1B.dat)
@@ -37,7 +40,7 @@ from sccm_gb300.basis import ModelSpace  # noqa: E402
 from sccm_gb300.formats import (mscheme_pairs, read_elem_axial, read_me1b,  # noqa: E402
                                 read_mscheme_binary, read_rho1b_dens, read_val, read_wf)
 
-REF = os.environ.get("SCCM_REF", "/root/reference")
+REF = os.environ.get("SCCM_REF", "")
 BETAS = (-10, 0, 10, 20)       # beta2 x 100
 
 
@@ -59,6 +62,8 @@ def rho1b_name(b1, b2):
 
 
 def main(out=os.path.join(HERE, "ge76_fixture.npz")):
+    if not REF or not os.path.isdir(REF):
+        raise SystemExit("set SCCM_REF to the root of the SCCM reference tree")
     orbits = read_val(f"{REF}/Codes/val/pf5g9.val")
     sp = ModelSpace(orbits, 4, 16, 28, 28)
     e0, spe = read_me1b(f"{REF}/Codes/int/GCN2850/SM_GCN2850_ME1B.dat")

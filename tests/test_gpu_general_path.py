@@ -1,0 +1,195 @@
+"""GPU (C-ABI) vs oracle on the general path and on the benchmark cases' own meshes.
+
+The general path is what a pair takes when its vacua mix protons and neutrons (the
+kernels then eliminate one n x n skew matrix and solve one n x n system per point
+instead of two compact species blocks). The reference's own HFB vacua with
+proton-neutron pairing (Ti48 / KB3G, data/Ti/*.wf) run it, and so do synthetic
+vacua whose random generator has proton-neutron entries (`pn_mix`).
+
+Tolerances, as in test_gpu_parity.py, in both arithmetic forms:
+  * norm kernel N(Omega): 1e-10 relative to max |N| over the compared points;
+  * the other observables: 1e-9 relative to max |column|.
+"""
+import numpy as np
+import pytest
+
+from sccm_gb300.basis import NOBS, Mesh
+from sccm_gb300.pnamp import ST_PIVOT_UNDERFLOW, PnampContext
+from sccm_gb300.synth import config, make_workload, ti48_workload
+from oracle.pnamp_oracle import Hamiltonian, kernel_triaxial
+from oracle.pool import zres_pool
+
+pytestmark = pytest.mark.gpu
+
+NORM_TOL = 1e-10
+OBS_TOL = 1e-9
+FORMS = ["fp64", "df64"]
+
+
+def ctx_for(w, mesh=None, form="fp64", **kw):
+    return PnampContext(w.sp, w.e0, w.t1b, w.recs, w.vbar, mesh or w.mesh, q2=w.q2, form=form, **kw)
+
+
+def assert_close(z_gpu, z_ref, rows=None):
+    if rows is not None:
+        z_gpu, z_ref = z_gpu[rows], z_ref[rows]
+    nref = np.abs(z_ref[:, 0]).max()
+    err = np.abs(z_gpu[:, 0] - z_ref[:, 0]).max() / nref
+    assert err <= NORM_TOL, f"norm kernel rel err {err:.2e}"
+    for io in range(1, NOBS):
+        scale = np.abs(z_ref[:, io]).max()
+        if scale == 0.0:
+            assert np.abs(z_gpu[:, io]).max() == 0.0, io
+            continue
+        e = np.abs(z_gpu[:, io] - z_ref[:, io]).max() / scale
+        assert e <= OBS_TOL, f"observable {io + 1}: rel err {e:.2e}"
+
+
+def cross_species(U, V):
+    h = U.shape[0] // 2
+    return max(np.abs(M[:h, h:]).max() for M in (U, V, U.T, V.T))
+
+
+@pytest.fixture(scope="module")
+def pfmix():
+    return make_workload("pf", 2, Mesh(2, 3, 2, 3), seed=404, pn_mix=True)
+
+
+def test_pn_mixed_vacua_mix_the_species(pfmix):
+    for U, V in pfmix.vacua:
+        assert cross_species(U, V) > 1e-2
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_pf_pn_mixed_pairs_match_oracle(pfmix, form):
+    w = pfmix
+    ham = Hamiltonian(w.e0, w.t1b, w.recs, w.vbar, w.q2, w.jops)
+    pairs = [(0, 1), (1, 1), (1, 0)]
+    with ctx_for(w, form=form) as ctx:
+        z, st = ctx.batch([(*w.vacua[i], *w.vacua[j]) for i, j in pairs])
+    for k, (i, j) in enumerate(pairs):
+        ref = kernel_triaxial(w.sp, ham, w.mesh, *w.vacua[i], *w.vacua[j])
+        assert_close(z[k], ref)
+        assert (st[k] & ~ST_PIVOT_UNDERFLOW).max() == 0
+
+
+@pytest.fixture(scope="module")
+def ti48():
+    return ti48_workload(Mesh(2, 3, 2, 5))
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_ti48_kb3g_pairs_on_triaxial_mesh_match_oracle(ti48, form):
+    """The reference's own vacua and interaction (n = 40, Z = 2, N = 6, proton-neutron
+    pairing). Bras 0, 1 and 7 (beta2 = -0.3, -0.2, 0.4) have V0 with LU pivot ratios
+    2e-6 ... 8e-5, so those pairs run the 2n x 2n Pfaffian; the others the reduced one."""
+    w = ti48
+    pairs = [(3, 5), (2, 6), (4, 4), (0, 3), (7, 4), (1, 5), (3, 7), (0, 1)]
+    for i, j in pairs:
+        assert cross_species(*w.vacua[i]) > 1e-3
+    with ctx_for(w, form=form) as ctx:
+        z, st = ctx.batch([(*w.vacua[i], *w.vacua[j]) for i, j in pairs])
+    for k, (i, j) in enumerate(pairs):
+        assert_close(z[k], zres_pool(w, w.mesh, i, j))
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_ti48_ill_conditioned_kets_match_high_precision(ti48, form):
+    """Kets with cond(U1) ~ 1e4-1e5 (vacua 0 and 1): the reference's sequence, which inverts
+    the rotated U1 at every point (PNAMP_Proj.f90:162-184), loses up to ~1e-8 of the gauge-
+    summed norm there, so the FP64 restatement cannot judge at 1e-10. The judge is the same
+    formula in 30-digit arithmetic (tests/golden/make_ti48_highprec.py) at the Euler points
+    where the FP64 sequence is worst; the GPU must be within 1e-10 of it."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ti48_highprec.npz"))
+    w = ti48
+    assert tuple(d["mesh"]) == (w.mesh.nalp, w.mesh.nbet, w.mesh.ngam, w.mesh.nfom)
+    pairs = sorted({(int(b), int(k)) for b, k, _ in d["cases"]})
+    with ctx_for(w, form=form) as ctx:
+        z, _ = ctx.batch([(*w.vacua[i], *w.vacua[j]) for i, j in pairs])
+    for (b, k, ie), want in zip(d["cases"], d["norm"]):
+        got = z[pairs.index((int(b), int(k)))][int(ie), 0]
+        err = abs(got - want) / abs(want)
+        assert err <= NORM_TOL, f"pair ({b},{k}) Euler point {ie}: rel err {err:.2e}"
+
+
+@pytest.fixture(scope="module")
+def cfg0():
+    """The sd case exactly: seed 1000, 8 x 16 x 8 Euler, 7 x 7 gauge, 50,176 points;
+    the oracle over every point on a process pool."""
+    w = config(0)
+    return w, zres_pool(w, w.mesh, 0, 1)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_sd_case_full_mesh_matches_oracle(cfg0, form):
+    w, ref = cfg0
+    assert w.mesh.n_euler * w.mesh.n_gauge == 50176
+    assert cross_species(*w.vacua[0]) > 1e-2
+    with ctx_for(w, form=form) as ctx:
+        r = ctx.pair(*w.vacua[0], *w.vacua[1])
+    assert_close(r.zres, ref)
+
+
+def _items_zres(ctx, w, pair_list, euler_idx):
+    import torch
+    dev = torch.device("cuda")
+    packed = PnampContext.pack_pairs([(*w.vacua[i], *w.vacua[j]) for i, j in pair_list])
+    uv = torch.from_numpy(packed).to(dev)
+    items = torch.tensor([[p, e] for p in range(len(pair_list)) for e in euler_idx], dtype=torch.int32, device=dev)
+    z = torch.zeros((len(pair_list), NOBS, ctx.n_euler, 2), dtype=torch.float64, device=dev)
+    st = torch.zeros((len(pair_list), ctx.n_euler), dtype=torch.int32, device=dev)
+    ctx.batch_items_device(len(pair_list), uv.data_ptr(), items.shape[0], items.data_ptr(), z.data_ptr(),
+                           st.data_ptr(), 0, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    zz = z.cpu().numpy()
+    return (zz[..., 0] + 1j * zz[..., 1]).transpose(0, 2, 1), st.cpu().numpy()
+
+
+def _config1_sample(mesh):
+    """Euler indices (beta outer, alpha, gamma inner) at the two largest and the two
+    smallest beta nodes and one in the middle, each at three (alpha, gamma) nodes."""
+    na, nb, ng = mesh.nalp, mesh.nbet_used, mesh.ngam
+    betas = [int(k) for k in np.argsort(mesh.beta[:nb])[::-1][:2]] + [nb // 2] + \
+            [int(k) for k in np.argsort(mesh.beta[:nb])[:2]]
+    ag = [(0, 0), (na // 2, ng - 1), (na - 1, ng // 3)]
+    return sorted({kb * na * ng + ka * ng + kg for kb in betas for ka, kg in ag})
+
+
+@pytest.fixture(scope="module", params=[False, True], ids=["split", "pnmix"])
+def cfg1(request):
+    """The pf case (20 deformed vacua, 10 x 20 x 10 Euler, 9 x 9 gauge) on a sample of
+    its Euler points that includes the largest beta nodes, for the first-last vacuum pair."""
+    w = config(1, pn_mix=request.param)
+    idx = _config1_sample(w.mesh)
+    return w, idx, zres_pool(w, w.mesh, 0, len(w.vacua) - 1, euler_subset=idx)
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_pf_case_mesh_sample_matches_oracle(cfg1, form):
+    w, idx, ref = cfg1
+    assert w.mesh.beta[:w.mesh.nbet_used].max() > 3.0   # beta close to pi is in the sample
+    with ctx_for(w, form=form) as ctx:
+        z, st = _items_zres(ctx, w, [(0, len(w.vacua) - 1)], idx)
+    assert_close(z[0], ref, rows=idx)
+    others = np.setdiff1d(np.arange(w.mesh.n_euler), idx)
+    assert np.abs(z[0][others]).max() == 0.0   # items not listed are not written
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_pfaffian_early_exit_value_and_status(pfmix, form):
+    """A Pfaffian matrix scale (Input%Cscale) so small that every pivot is below the
+    reference's 1e-13 (PNAMP_Proj.f90:290,333): the oracle's ZPfaffianF returns 0 with its
+    exit flag at the first step, and the GPU must give N = 0 (hence ZRES = 0) with
+    PNAMP_ST_PIVOT_UNDERFLOW at every Euler point."""
+    w = pfmix
+    cscale = 1e-16
+    ham = Hamiltonian(w.e0, w.t1b, w.recs, w.vbar, w.q2, w.jops)
+    log = []
+    ref = kernel_triaxial(w.sp, ham, w.mesh, *w.vacua[0], *w.vacua[1], cscale=cscale, point_log=log)
+    assert all(abs(pf) == 0.0 for _, _, _, pf, _ in log)
+    assert np.abs(ref).max() == 0.0
+    with ctx_for(w, form=form, cscale=cscale) as ctx:
+        r = ctx.pair(*w.vacua[0], *w.vacua[1])
+    assert np.abs(r.zres).max() == 0.0
+    assert np.all(r.status & ST_PIVOT_UNDERFLOW)
