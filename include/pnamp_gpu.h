@@ -56,12 +56,24 @@ extern "C" {
 #define PNAMP_FORM_DF64 1   /* Pfaffian, LU, solves, densities and contractions in double-float
                                (pairs of FP32, ~48-bit significand) on the FP32 pipes; per-Euler
                                preparation, the Pfaffian product and all reductions stay FP64 */
+#define PNAMP_FORM_TC3 2    /* PNAMP_FORM_DF64 with the two-body contraction of HFB_Energy_COMPLEX
+                               (PNAMP_Energy_OpenMP.f90:31-90) recast as dense block GEMMs on the
+                               tensor cores (tcgen05, bf16 inputs, FP32 accumulation): each value
+                               as two bf16 terms, three products ("BF16x3", ~1e-5 relative) */
+#define PNAMP_FORM_TC6 3    /* the same with three bf16 terms and six products ("BF16x6", ~1e-7).
+                               Both tensor-core forms apply to pnamp_pair, pnamp_batch(_device) and
+                               pnamp_batch_items_device (without gauge output; norm-only outputs give
+                               PNAMP_ERR_STATE) and stage the densities of up to min(24 GiB, half the
+                               free device memory) of points per launch; the other entry points
+                               compute in the PNAMP_FORM_DF64 arithmetic under these forms */
 
 /* per-Euler-point status bits (OR over the gauge points of that Euler point) */
 #define PNAMP_ST_PIVOT_UNDERFLOW 1  /* Pfaffian pivot |ss| <= 1e-13: norm set to 0 (PNAMP_Proj.f90:290,333) */
 #define PNAMP_ST_SINGULAR_T22 2     /* exact zero pivot in the LU of T22 */
 #define PNAMP_ST_NONFINITE 4        /* a non-finite value reached ZRES */
 #define PNAMP_ST_SINGULAR_U 8       /* the pair's U0 or U1 is singular */
+#define PNAMP_ST_CONTRACTION 16     /* tensor-core forms: the contraction kernel gave up (a bounded wait
+                                       ran out); the energy ZRES(:, 7) of this point is not valid */
 
 /* Model space: the m-scheme `tnljm` arrays (VAPHFB_Par.f90:39-43), ordered
  * protons (t = -1) first, then neutrons (t = +1); within a species orbits in
@@ -284,6 +296,15 @@ int pnamp_project_q_device(pnamp_ctx *ctx, int npairs, const double *d_zres, int
 
 /* Synchronise the context's work; returns the first CUDA error seen. */
 int pnamp_sync(pnamp_ctx *ctx);
+
+/* Stage timing (no counterpart in the reference, whose timers are commented out,
+ * PNAMP_Kernel3D.f90:189-192,241-242): with `on` set, each later pnamp_batch_device /
+ * pnamp_batch_items_device call records CUDA events around its launches on the launching
+ * stream; pnamp_stage_times waits for the last call's events and writes the summed
+ * milliseconds of its stages to ms[4] = {setup, point kernel, tensor-core contraction,
+ * contraction sum into ZRES}, returning 4 (or an error code). */
+int pnamp_set_timing(pnamp_ctx *ctx, int on);
+int pnamp_stage_times(pnamp_ctx *ctx, double *ms);
 
 /* Free the context and its device memory. */
 void pnamp_free(pnamp_ctx *ctx);

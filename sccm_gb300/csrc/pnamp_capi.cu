@@ -56,6 +56,28 @@ struct pnamp_ctx {
     uint32_t *d_r2q = nullptr;
     double *d_r2acc = nullptr, *d_r2out = nullptr;
     long long r2acc_cap = 0, r2out_cap = 0;
+    // tensor-core contraction of the two-body energy (contract_tc.cu): bf16 terms per value
+    // (0 = the record loop in the point kernel), tables built on first use, staging buffers
+    int tc_splits = 0;
+    std::vector<uint32_t> h_rec_idx;
+    std::vector<double> h_rec_v;
+    bool tc_built = false;
+    int tc_nk = 0, tc_nph = 0, tc_kmax = 0;
+    long long tc_rows = 0;
+    std::vector<TcGroup> tc_groups;
+    std::vector<int> tc_src;
+    TcGroup *d_tc_groups = nullptr;
+    int *d_tc_src = nullptr;
+    unsigned short *d_tc_mat[3] = {nullptr, nullptr, nullptr};
+    unsigned short *d_tc_x[3] = {nullptr, nullptr, nullptr}, *d_tc_y[3] = {nullptr, nullptr, nullptr};
+    double *d_tc_w = nullptr, *d_tc_e2 = nullptr;
+    int *d_tc_err = nullptr;
+    long long tc_cap_pts = 0;
+    int nsm = 0;
+    // per-stage CUDA-event timing of the last pnamp_batch_device / items call (pnamp_set_timing)
+    int timing = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::array<int, 3>> ev_marks;   // (stage, start event, end event)
 };
 
 namespace {
@@ -310,6 +332,295 @@ int build_r2(int n, const int *t, const int *nn1, const int *l, const int *tj, c
     return PNAMP_OK;
 }
 
+// ---------------------------------------------------------------- stage timing
+// Events around each launch of a batch call, on the launching stream, when timing is on.
+enum { kStageSetup = 0, kStagePoints = 1, kStageContract = 2, kStageFinish = 3, kStages = 4 };
+int stage_begin(pnamp_ctx *c, cudaStream_t st) {
+    if (!c->timing) return -1;
+    const int k = (int)c->ev_marks.size();
+    while ((int)c->ev_pool.size() < 2 * (k + 1)) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return -1;
+        c->ev_pool.push_back(e);
+    }
+    if (cudaEventRecord(c->ev_pool[2 * k], st) != cudaSuccess) return -1;
+    return k;
+}
+void stage_end(pnamp_ctx *c, cudaStream_t st, int k, int stage) {
+    if (k < 0) return;
+    if (cudaEventRecord(c->ev_pool[2 * k + 1], st) == cudaSuccess) c->ev_marks.push_back({stage, 2 * k, 2 * k + 1});
+}
+
+// ---------------------------------------------------------------- tensor-core contraction
+// Tables of the two bilinear forms the two-body energy regroups into (contract_tc.cu):
+// particle-hole entries s_e = rho(r, c), labelled (m_r - m_c, t_r - t_c, parity) and packed
+// with their negated labels into groups of <= kTcGroupCap storage entries; particle-particle
+// pair entries (i < j) labelled (m_i + m_j, t_i + t_j, parity) and packed the same way. Each
+// group's storage range is padded to 64 entries (one TMA/UMMA K chunk); its square matrix
+// (rows = output entries, columns = operand entries) is stacked into one [rows][kmax]
+// array and kept as three bf16 terms t0 + t1 + t2 of each FP64 value.
+constexpr int kTcGroupCap = 256;
+
+uint16_t bf16_rn_host(float f) {
+    uint32_t b;
+    memcpy(&b, &f, 4);
+    if ((b & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;       // NaN
+    b += 0x7fffu + ((b >> 16) & 1u);                          // round to nearest, ties to even
+    return (uint16_t)(b >> 16);
+}
+double bf16_value(uint16_t h) {
+    const uint32_t b = (uint32_t)h << 16;
+    float f;
+    memcpy(&f, &b, 4);
+    return (double)f;
+}
+
+template <class Key>
+std::vector<std::vector<Key>> pack_groups(const std::vector<std::vector<Key>> &units,
+                                          const std::map<Key, std::vector<int>> &members) {
+    // first fit, largest units first (ties keep label order)
+    std::vector<int> order(units.size());
+    for (size_t i = 0; i < units.size(); ++i) order[i] = (int)i;
+    auto size_of = [&](int u) {
+        int sz = 0;
+        for (const Key &k : units[u]) sz += (int)members.at(k).size();
+        return sz;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return size_of(a) > size_of(b); });
+    std::vector<std::vector<Key>> groups;
+    std::vector<int> fill;
+    for (int u : order) {
+        const int sz = size_of(u);
+        size_t g = 0;
+        for (; g < groups.size(); ++g)
+            if (fill[g] + sz <= kTcGroupCap) break;
+        if (g == groups.size()) {
+            groups.emplace_back();
+            fill.push_back(0);
+        }
+        groups[g].insert(groups[g].end(), units[u].begin(), units[u].end());
+        fill[g] += sz;
+    }
+    return groups;
+}
+
+int build_tc(pnamp_ctx *c) {
+    const int n = c->p.n;
+    using L3 = std::array<int, 3>;
+    std::map<L3, std::vector<int>> ph, pp;   // label -> entries (r << 8 | c), row-major order
+    for (int r = 0; r < n; ++r)
+        for (int q = 0; q < n; ++q)
+            ph[{c->sp_tm[r] - c->sp_tm[q], c->sp_t[r] - c->sp_t[q], (c->sp_l[r] + c->sp_l[q]) & 1}].push_back(
+                (r << 8) | q);
+    for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j)
+            pp[{c->sp_tm[i] + c->sp_tm[j], c->sp_t[i] + c->sp_t[j], (c->sp_l[i] + c->sp_l[j]) & 1}].push_back(
+                (i << 8) | j);
+    std::vector<std::vector<L3>> ph_units, pp_units;
+    for (const auto &kv : ph) {
+        const L3 L = kv.first, N = {-L[0], -L[1], L[2]};
+        if (N < L && ph.count(N)) continue;          // the pair (N, L) was made at N
+        ph_units.push_back(N == L || !ph.count(N) ? std::vector<L3>{L} : std::vector<L3>{L, N});
+    }
+    for (const auto &kv : pp) pp_units.push_back({kv.first});
+    const auto ph_groups = pack_groups(ph_units, ph), pp_groups = pack_groups(pp_units, pp);
+
+    std::vector<int> pos_ph((size_t)n * n, -1), pos_pp((size_t)n * n, -1);
+    c->tc_groups.clear();
+    c->tc_src.clear();
+    int off = 0, rowbase = 0, kmax = 0;
+    auto place = [&](const std::vector<std::vector<L3>> &groups, const std::map<L3, std::vector<int>> &mem,
+                     std::vector<int> &pos, int kind, int yoff0) {
+        for (const auto &g : groups) {
+            TcGroup G;
+            G.kind = kind;
+            G.off = off;
+            int d = 0;
+            for (const L3 &k : g)
+                for (int e : mem.at(k)) {
+                    pos[(size_t)(e >> 8) * n + (e & 255)] = off + d++;
+                    c->tc_src.push_back(e);
+                }
+            G.dpad = (d + 63) / 64 * 64;
+            for (int k = d; k < G.dpad; ++k) c->tc_src.push_back(-1);
+            G.rowbase = rowbase;
+            G.yoff = kind ? off - yoff0 : 0;
+            off += G.dpad;
+            rowbase += G.dpad;
+            kmax = std::max(kmax, G.dpad);
+            c->tc_groups.push_back(G);
+        }
+    };
+    place(ph_groups, ph, pos_ph, 0, 0);
+    c->tc_nph = off;
+    place(pp_groups, pp, pos_pp, 1, c->tc_nph);
+    c->tc_nk = off;
+    c->tc_kmax = kmax;
+    c->tc_rows = rowbase;
+    // group of each storage position
+    std::vector<int> grp_of(off, -1);
+    for (size_t g = 0; g < c->tc_groups.size(); ++g)
+        for (int k = 0; k < c->tc_groups[g].dpad; ++k) grp_of[c->tc_groups[g].off + k] = (int)g;
+    std::vector<double> mat((size_t)rowbase * kmax, 0.0);
+    auto add = [&](int e1, int e2, double v) {  // storage positions (row, column) of one group
+        const TcGroup &G = c->tc_groups[grp_of[e1]];
+        mat[(size_t)(G.rowbase + e1 - G.off) * kmax + (e2 - G.off)] += v;
+    };
+    auto ph_at = [&](int r, int q) { return pos_ph[(size_t)r * n + q]; };
+    auto pp_at = [&](int i, int j) { return pos_pp[(size_t)i * n + j]; };
+    for (size_t e = 0; e < c->h_rec_idx.size(); ++e) {
+        const uint32_t pk = c->h_rec_idx[e];
+        const int i = pk & 0xff, j = (pk >> 8) & 0xff, k = (pk >> 16) & 0xff, l = pk >> 24;
+        const double V = c->h_rec_v[e];
+        const bool d = (i + j) != (k + l);
+        // particle hole: V rho_ki rho_lj - V rho_li rho_kj + d (V rho_ik rho_jl - V rho_jk rho_il)
+        // as s_e1 M s_e2 with the second factor read transposed
+        add(ph_at(k, i), ph_at(l, j), V);
+        add(ph_at(l, i), ph_at(k, j), -V);
+        if (d) {
+            add(ph_at(i, k), ph_at(j, l), V);
+            add(ph_at(j, k), ph_at(i, l), -V);
+        }
+        // particle particle: V/4 (K01_ij K10_kl + d K01_kl K10_ij)
+        if (i >= j || k >= l) return PNAMP_ERR_ARG;
+        add(pp_at(i, j), pp_at(k, l), 0.25 * V);
+        if (d) add(pp_at(k, l), pp_at(i, j), 0.25 * V);
+    }
+    std::vector<uint16_t> terms[3];
+    for (auto &t : terms) t.resize(mat.size());
+    for (size_t q = 0; q < mat.size(); ++q) {
+        double r = mat[q];
+        for (int sp = 0; sp < 3; ++sp) {
+            terms[sp][q] = bf16_rn_host((float)r);
+            r -= bf16_value(terms[sp][q]);
+        }
+    }
+    CK(cudaMalloc(&c->d_tc_groups, c->tc_groups.size() * sizeof(TcGroup)));
+    CK(cudaMemcpy(c->d_tc_groups, c->tc_groups.data(), c->tc_groups.size() * sizeof(TcGroup),
+                  cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&c->d_tc_src, c->tc_src.size() * sizeof(int)));
+    CK(cudaMemcpy(c->d_tc_src, c->tc_src.data(), c->tc_src.size() * sizeof(int), cudaMemcpyHostToDevice));
+    for (int sp = 0; sp < 3; ++sp) {
+        CK(cudaMalloc(&c->d_tc_mat[sp], mat.size() * sizeof(uint16_t)));
+        CK(cudaMemcpy(c->d_tc_mat[sp], terms[sp].data(), mat.size() * sizeof(uint16_t), cudaMemcpyHostToDevice));
+    }
+    CK(cudaMalloc(&c->d_tc_err, sizeof(int)));
+    CK(prepare_contract());
+    c->tc_built = true;
+    return PNAMP_OK;
+}
+
+// Staging for `pts` kernel points: X and Y rows per bf16 term, weights, E2.
+int ensure_tc_staging(pnamp_ctx *c, long long pts) {
+    if (pts <= c->tc_cap_pts) return PNAMP_OK;
+    for (int sp = 0; sp < 3; ++sp) {
+        if (c->d_tc_x[sp]) cudaFree(c->d_tc_x[sp]);
+        if (c->d_tc_y[sp]) cudaFree(c->d_tc_y[sp]);
+        c->d_tc_x[sp] = c->d_tc_y[sp] = nullptr;
+    }
+    if (c->d_tc_w) cudaFree(c->d_tc_w);
+    if (c->d_tc_e2) cudaFree(c->d_tc_e2);
+    c->d_tc_w = c->d_tc_e2 = nullptr;
+    c->tc_cap_pts = 0;
+    const int npp = c->tc_nk - c->tc_nph;
+    for (int sp = 0; sp < c->tc_splits; ++sp) {
+        CK(cudaMalloc(&c->d_tc_x[sp], (size_t)pts * 2 * c->tc_nk * sizeof(uint16_t)));
+        CK(cudaMalloc(&c->d_tc_y[sp], (size_t)pts * 2 * npp * sizeof(uint16_t)));
+    }
+    CK(cudaMalloc(&c->d_tc_w, (size_t)pts * 2 * sizeof(double)));
+    CK(cudaMalloc(&c->d_tc_e2, (size_t)pts * 2 * sizeof(double)));
+    c->tc_cap_pts = pts;
+    return PNAMP_OK;
+}
+
+// Points per launch of the tensor-core forms: the staging of one chunk stays under
+// min(24 GiB, half the free device memory), and at least one pair (or item) fits.
+long long tc_chunk_points(pnamp_ctx *c, long long unit_pts) {
+    const long long per_pt = (long long)c->tc_splits * 2 * (2LL * c->tc_nk - c->tc_nph) * 2 + 32;
+    size_t fr = 0, tot = 0;
+    long long budget = 24LL << 30;
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess) budget = std::min<long long>(budget, (long long)(fr / 2));
+    const long long units = std::max<long long>(1, budget / per_pt / unit_pts);
+    return units * unit_pts;
+}
+
+// The tensor-core forms: setup, then per chunk the point kernel (double-float algebra, densities
+// staged), the contraction and the per-item sum into ZRES(:, 7). `items` selects (pair, Euler
+// point) entries as pnamp_batch_items_device does; NULL means every Euler point of every pair.
+int tc_run(pnamp_ctx *c, int npairs, const double *d_uv, double *d_zres, int *d_status, cudaStream_t st,
+           const int *items, long long nitems) {
+    if (c->p.norm_only) return PNAMP_ERR_STATE;
+    int rc;
+    if (!c->tc_built && (rc = build_tc(c)) != PNAMP_OK) return rc;
+    int mk = stage_begin(c, st);
+    CK(launch_setup(c->p, npairs, d_uv, c->d_pairbuf, st));
+    stage_end(c, st, mk, kStageSetup);
+    const int P = c->p.n_euler, G = c->p.n_gauge;
+    const long long total_items = items ? nitems : (long long)npairs * P;
+    const long long chunk_pts =
+        std::min<long long>(tc_chunk_points(c, items ? (long long)G : (long long)P * G), total_items * G);
+    if ((rc = ensure_tc_staging(c, chunk_pts)) != PNAMP_OK) return rc;
+    const long long chunk_items = chunk_pts / G;
+    Params q = c->p;
+    q.tc_splits = c->tc_splits;
+    q.tc_nk = c->tc_nk;
+    q.tc_nph = c->tc_nph;
+    q.tc_src = c->d_tc_src;
+    for (int sp = 0; sp < 3; ++sp) {
+        q.tc_x[sp] = c->d_tc_x[sp];
+        q.tc_y[sp] = c->d_tc_y[sp];
+    }
+    q.tc_w = c->d_tc_w;
+    TcArgs a;
+    memset(&a, 0, sizeof(a));
+    a.splits = c->tc_splits;
+    a.ngroups = (int)c->tc_groups.size();
+    a.nk = c->tc_nk;
+    a.npp = c->tc_nk - c->tc_nph;
+    a.groups = c->d_tc_groups;
+    for (int sp = 0; sp < 3; ++sp) {
+        a.x[sp] = c->d_tc_x[sp];
+        a.y[sp] = c->d_tc_y[sp];
+    }
+    a.e2 = c->d_tc_e2;
+    a.err = c->d_tc_err;
+    const void *mat[3] = {c->d_tc_mat[0], c->d_tc_mat[1], c->d_tc_mat[2]};
+    const long long zstride = 2LL * kNobs * P;
+    for (long long i0 = 0; i0 < total_items; i0 += chunk_items) {
+        const long long cnt = std::min<long long>(chunk_items, total_items - i0);
+        CK(cudaMemsetAsync(c->d_tc_err, 0, sizeof(int), st));
+        a.npts = cnt * G;
+        if (items) {
+            const int2 *it = reinterpret_cast<const int2 *>(items) + i0;
+            const int grid = (int)std::min<long long>(c->grid_form[1], cnt);
+            mk = stage_begin(c, st);
+            CK(launch_points(q, npairs, c->d_pairbuf, c->d_scratch, grid, d_zres, d_status, st, it, cnt));
+            stage_end(c, st, mk, kStagePoints);
+            mk = stage_begin(c, st);
+            CK(launch_contract(a, mat, c->tc_rows, c->tc_kmax, c->nsm, st));
+            stage_end(c, st, mk, kStageContract);
+            mk = stage_begin(c, st);
+            CK(launch_contract_finish(npairs, P, G, cnt, it, c->d_tc_w, c->d_tc_e2, d_zres, d_status, c->d_tc_err,
+                                      st));
+            stage_end(c, st, mk, kStageFinish);
+        } else {
+            const int pair0 = (int)(i0 / P), np = (int)(cnt / P);
+            mk = stage_begin(c, st);
+            CK(launch_points(q, np, c->d_pairbuf + (long long)pair0 * c->p.pl.stride, c->d_scratch,
+                             c->grid_form[1], d_zres + pair0 * zstride, d_status + (long long)pair0 * P, st));
+            stage_end(c, st, mk, kStagePoints);
+            mk = stage_begin(c, st);
+            CK(launch_contract(a, mat, c->tc_rows, c->tc_kmax, c->nsm, st));
+            stage_end(c, st, mk, kStageContract);
+            mk = stage_begin(c, st);
+            CK(launch_contract_finish(np, P, G, cnt, nullptr, c->d_tc_w, c->d_tc_e2, d_zres + pair0 * zstride,
+                                      d_status + (long long)pair0 * P, c->d_tc_err, st));
+            stage_end(c, st, mk, kStageFinish);
+        }
+    }
+    return PNAMP_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -335,9 +646,21 @@ const char *pnamp_version(void) { return "sccm_gb300 pnamp 0.1 (sm_103a, fp64)";
 int pnamp_n_euler(const pnamp_ctx *ctx) { return ctx ? ctx->p.n_euler : -1; }
 
 int pnamp_set_form(pnamp_ctx *ctx, int form) {
-    if (!ctx || (form != PNAMP_FORM_FP64 && form != PNAMP_FORM_DF64)) return PNAMP_ERR_ARG;
-    ctx->p.form = form;
-    return PNAMP_OK;
+    if (!ctx) return PNAMP_ERR_ARG;
+    switch (form) {
+        case PNAMP_FORM_FP64:
+        case PNAMP_FORM_DF64:
+            ctx->p.form = form;
+            ctx->tc_splits = 0;
+            return PNAMP_OK;
+        case PNAMP_FORM_TC3:
+        case PNAMP_FORM_TC6:
+            ctx->p.form = PNAMP_FORM_DF64;   // the per-point algebra of the mixed form
+            ctx->tc_splits = form == PNAMP_FORM_TC3 ? 2 : 3;
+            return PNAMP_OK;
+        default:
+            return PNAMP_ERR_ARG;
+    }
 }
 
 int pnamp_set_outputs(pnamp_ctx *ctx, int outputs) {
@@ -355,6 +678,13 @@ void pnamp_free(pnamp_ctx *ctx) {
     for (void *q : {(void *)ctx->d_pairbuf, (void *)ctx->d_scratch, (void *)ctx->d_uv, (void *)ctx->d_zres,
                     (void *)ctx->d_status, (void *)ctx->d_proj, (void *)ctx->d_projq})
         if (q) cudaFree(q);
+    for (int sp = 0; sp < 3; ++sp)
+        for (void *q : {(void *)ctx->d_tc_mat[sp], (void *)ctx->d_tc_x[sp], (void *)ctx->d_tc_y[sp]})
+            if (q) cudaFree(q);
+    for (void *q : {(void *)ctx->d_tc_groups, (void *)ctx->d_tc_src, (void *)ctx->d_tc_w, (void *)ctx->d_tc_e2,
+                    (void *)ctx->d_tc_err})
+        if (q) cudaFree(q);
+    for (cudaEvent_t e : ctx->ev_pool) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -436,6 +766,8 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
         rec_idx.swap(gi);
         rec_v.swap(gv);
     }
+    std::vector<uint32_t> h_rec_idx = rec_idx;
+    std::vector<double> h_rec_v = rec_v;
     // one-body tables
     std::vector<int> t1b_idx;
     std::vector<double> t1b_val;
@@ -587,6 +919,8 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
             UP(val, ot.r1b_val);
         }
         for (size_t e = 3; e < euler.size(); e += 4) c->euler_w.push_back(euler[e]);
+        c->h_rec_idx.swap(h_rec_idx);
+        c->h_rec_v.swap(h_rec_v);
         c->sp_t.assign(sp->t, sp->t + n);
         c->sp_n.assign(sp->n, sp->n + n);
         c->sp_l.assign(sp->l, sp->l + n);
@@ -619,6 +953,7 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
         }
         c->grid_form[form] = nsm * per_sm;
     }
+    c->nsm = nsm;
     p.form = 0;
     p.norm_only = 0;
     p.n_r2q = 0;  // two-body density launches set their own copy
@@ -668,8 +1003,14 @@ int pnamp_batch_device(pnamp_ctx *c, int npairs, const double *d_uv, double *d_z
     int rc = ensure_pairs(c, npairs);
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
+    c->ev_marks.clear();
+    if (c->tc_splits) return tc_run(c, npairs, d_uv, d_zres, d_status, st, nullptr, 0);
+    int mk = stage_begin(c, st);
     CK(launch_setup(c->p, npairs, d_uv, c->d_pairbuf, st));
+    stage_end(c, st, mk, kStageSetup);
+    mk = stage_begin(c, st);
     CK(launch_points(c->p, npairs, c->d_pairbuf, c->d_scratch, c->grid_form[c->p.form], d_zres, d_status, st));
+    stage_end(c, st, mk, kStagePoints);
     return PNAMP_OK;
 }
 
@@ -681,6 +1022,11 @@ int pnamp_batch_items_device(pnamp_ctx *c, int npairs, const double *d_uv, long 
     int rc = ensure_pairs(c, npairs);
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
+    c->ev_marks.clear();
+    if (c->tc_splits) {
+        if (d_gauge_out) return PNAMP_ERR_STATE;  // per-gauge H/N would lack the contracted energy
+        return tc_run(c, npairs, d_uv, d_zres, d_status, st, d_items, nitems);
+    }
     CK(launch_setup(c->p, npairs, d_uv, c->d_pairbuf, st));
     const int grid = (int)std::min<long long>(c->grid_form[c->p.form], nitems);
     CK(launch_points(c->p, npairs, c->d_pairbuf, c->d_scratch, grid, d_zres, d_status, st,
@@ -1076,6 +1422,25 @@ int pnamp_sync(pnamp_ctx *c) {
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaGetLastError());
     return PNAMP_OK;
+}
+
+int pnamp_set_timing(pnamp_ctx *c, int on) {
+    if (!c) return PNAMP_ERR_ARG;
+    c->timing = on ? 1 : 0;
+    c->ev_marks.clear();
+    return PNAMP_OK;
+}
+
+int pnamp_stage_times(pnamp_ctx *c, double *ms) {
+    if (!c || !ms) return PNAMP_ERR_ARG;
+    for (int k = 0; k < kStages; ++k) ms[k] = 0.0;
+    for (const auto &m : c->ev_marks) {
+        float t = 0.f;
+        CK(cudaEventSynchronize(c->ev_pool[m[2]]));
+        CK(cudaEventElapsedTime(&t, c->ev_pool[m[1]], c->ev_pool[m[2]]));
+        ms[m[0]] += t;
+    }
+    return kStages;
 }
 
 }  // extern "C"

@@ -103,6 +103,33 @@ struct Params {
     int n_r2q;
     const uint32_t *r2q;
     double *r2acc;
+    // tensor-core contraction (contract_tc.cu): tc_splits = 0 runs the record loop here;
+    // 2 or 3 makes the point kernel write each gauge point's density rows as that many bf16
+    // terms instead (X: tc_nk entries, ph part first, pp part from tc_nph; Y: the pp
+    // epilogue vector, tc_nk - tc_nph entries) and its weight N / NFOM^2 (0 when T22 was
+    // singular); point p of a launch is item * n_gauge + gauge index
+    int tc_splits, tc_nk, tc_nph;
+    const int *tc_src;         // [tc_nk]: r << 8 | c (ph entries), i << 8 | j (pp, i < j), -1 padding
+    unsigned short *tc_x[3], *tc_y[3];
+    double *tc_w;
+};
+
+// One group of the contraction: a contiguous range [off, off + dpad) of the X row (and, for
+// a pp group, [yoff, yoff + dpad) of the Y row), whose square matrix occupies rows
+// [rowbase, rowbase + dpad) of the stacked bf16 matrices (columns 0..dpad-1).
+struct TcGroup {
+    int kind;      // 0 particle-hole (epilogue vector = X), 1 particle-particle (epilogue vector = Y)
+    int off, dpad, rowbase, yoff;
+};
+struct TcArgs {
+    int splits;
+    int ngroups;
+    long long npts;
+    int nk, npp;
+    const TcGroup *groups;
+    const unsigned short *x[3], *y[3];
+    double *e2;        // [npts][2]
+    int *err;
 };
 
 // Contexts of one multi-context launch, passed by value (kernel parameter space).
@@ -135,5 +162,14 @@ cudaError_t set_point_smem(int form, int bytes);
 cudaError_t point_blocks_per_sm(int form, int smem_bytes, int *per_sm);
 int setup_smem_bytes(int n);
 cudaError_t prepare_setup(int n);
+// tensor-core contraction (contract_tc.cu)
+cudaError_t prepare_contract();
+int tc_smem_bytes(int splits);
+int tc_chunk_rows(int splits);
+cudaError_t launch_contract(const TcArgs &a, const void *const *mat, long long mat_rows, int kmax, int grid,
+                            cudaStream_t st);
+cudaError_t launch_contract_finish(int npairs, int n_euler, int n_gauge, long long nitems, const int2 *items,
+                                   const double *w, const double *e2, double *zres, int *status, const int *err,
+                                   cudaStream_t st);
 
 }  // namespace pnamp

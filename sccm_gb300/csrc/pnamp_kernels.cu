@@ -25,10 +25,28 @@
 //   T22 = V0^T A V1 + U0^T A* U1 = sum_s e^{+-i phi_s} (species partials),
 //   rho = D (R V1 T22^-1) V0^T, kappa10 = D (R V1 T22^-1) U0^T,
 //   kappa01 = -D* (R* U1 T22^-1) V0^T.
+#include <cuda_bf16.h>
+
 #include "pnamp_df64.cuh"
 #include "pnamp_internal.h"
 
 namespace pnamp {
+
+// A value as S = 2 or 3 bf16 terms t0 + t1 (+ t2), each the bf16 rounding of what the
+// previous terms leave (8 significant bits each: ~2^-17 relative left for S = 2, ~2^-25 for
+// S = 3). v - t0 is exact in FP32 (t0 is v rounded to 8 bits); the double-float low word
+// enters the first remainder.
+__device__ __forceinline__ void bf16_terms(dd v, int S, unsigned short (&t)[3]) {
+    const __nv_bfloat16 b0 = __float2bfloat16_rn(v.hi);
+    const float r1 = __fadd_rn(__fsub_rn(v.hi, __bfloat162float(b0)), v.lo);
+    const __nv_bfloat16 b1 = __float2bfloat16_rn(r1);
+    const float r2 = __fsub_rn(r1, __bfloat162float(b1));
+    t[0] = __bfloat16_as_ushort(b0);
+    t[1] = __bfloat16_as_ushort(b1);
+    t[2] = S > 2 ? __bfloat16_as_ushort(__float2bfloat16_rn(r2)) : (unsigned short)0;
+}
+__device__ __forceinline__ dd as_dd(double v) { return dd_from(v); }
+__device__ __forceinline__ dd as_dd(dd v) { return v; }
 
 // ------------------------------------------------------------------ scalars
 __device__ __forceinline__ double sabs1(double a) { return fabs(a); }
@@ -822,7 +840,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                                            int pair, int ie, bool reload, double *__restrict__ zres,
                                            int *__restrict__ status, double *__restrict__ gout = nullptr,
                                            double *__restrict__ r1out = nullptr,
-                                           double *__restrict__ r2out = nullptr) {
+                                           double *__restrict__ r2out = nullptr, long long pt0 = 0) {
     using A = Ar<Z>;
     using R = typename A::R;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -878,6 +896,10 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 zout[2LL * (io * p.n_euler + ie) + 1] = 0.0;
             }
             if (threadIdx.x == 0) status[(long long)pair * p.n_euler + ie] = 8;
+            for (int g = threadIdx.x; g < (p.tc_splits ? p.n_gauge : 0); g += blockDim.x) {
+                p.tc_w[2 * (pt0 + g)] = 0.0;
+                p.tc_w[2 * (pt0 + g) + 1] = 0.0;
+            }
             return;
         }
         if (reload) {
@@ -1258,7 +1280,44 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     v = warp_sum(v);
                     if (lane == 0) pw[slot * nw + wid] = v;
                 };
-                {   // two-body energy, exact regrouping of the 8-term sum of
+                if (p.tc_splits) {
+                    // tensor-core contraction: this gauge point's operand rows X[2 pt + ri] (rho
+                    // entries, then K10 pairs) and epilogue rows Y[2 pt + ri] (K01 pairs) as bf16
+                    // terms; contract_tc.cu forms the two bilinear forms for the whole launch
+                    const long long pt = pt0 + lp * p.nfom + ln;
+                    const int S = p.tc_splits, nk = p.tc_nk, npp = p.tc_nk - p.tc_nph;
+                    for (int e = threadIdx.x; e < nk; e += blockDim.x) {
+                        const int src = p.tc_src[e];
+                        Z v = zero, y = zero;
+                        if (src >= 0) {
+                            const int r = src >> 8, c = src & 255;
+                            if (e < p.tc_nph) {
+                                v = rho[r * ld + c];
+                            } else {
+                                v = Kc[c * ld + r];   // K10_rc, r < c
+                                y = Kc[r * ld + c];   // K01_rc
+                            }
+                        }
+                        unsigned short tr[3], ti[3];
+                        bf16_terms(as_dd(v.x), S, tr);
+                        bf16_terms(as_dd(v.y), S, ti);
+                        for (int sp = 0; sp < S; ++sp) {
+                            p.tc_x[sp][(2 * pt) * nk + e] = tr[sp];
+                            p.tc_x[sp][(2 * pt + 1) * nk + e] = ti[sp];
+                        }
+                        if (e >= p.tc_nph) {
+                            bf16_terms(as_dd(y.x), S, tr);
+                            bf16_terms(as_dd(y.y), S, ti);
+                            const int ey = e - p.tc_nph;
+                            for (int sp = 0; sp < S; ++sp) {
+                                p.tc_y[sp][(2 * pt) * npp + ey] = tr[sp];
+                                p.tc_y[sp][(2 * pt + 1) * npp + ey] = ti[sp];
+                            }
+                        }
+                    }
+                    put(0, 0.0);
+                    put(1, 0.0);
+                } else {   // two-body energy, exact regrouping of the 8-term sum of
                     // PNAMP_Energy_OpenMP.f90:40-78:
                     // V[rho_ki rho_lj - rho_li rho_kj + d(rho_ik rho_jl - rho_jk rho_il)]
                     // + V/4 [K01_ij K10_kl + d K01_kl K10_ij],  K_xy = kappa_xy - kappa_yx
@@ -1358,6 +1417,13 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     const zc ekin = mk(get(4), get(5));
                     zc hg = mk(0.0, 0.0);  // H/N at this gauge point (0 when not computed)
                     if (!p.norm_only && !sing) hg = ekin + mk(get(6), get(7)) + mk(p.e0, 0.0);
+                    if (p.tc_splits && lane == 0) {   // w = N / NFOM^2 of this gauge point, 0 if not evaluated
+                        const long long pt = pt0 + lp * p.nfom + ln;
+                        const double inv = 1.0 / ((double)p.nfom * p.nfom);
+                        const bool use = !p.norm_only && !sing;
+                        p.tc_w[2 * pt] = use ? inv * norm.x : 0.0;
+                        p.tc_w[2 * pt + 1] = use ? inv * norm.y : 0.0;
+                    }
                     if (lane == 0) {
                         acc[0] = acc[0] + norm;
                         if (r2out) {
@@ -1460,7 +1526,8 @@ point_kernel(Params p, int npairs, const double *__restrict__ pairbuf, zc *scrat
             pair = (int)(item / p.n_euler);
             ie = (int)(item % p.n_euler);
         }
-        point_item<Z>(p, pairbuf, slot, pair, ie, pair != cur_pair, zres, status, gout, r1out, r2out);
+        point_item<Z>(p, pairbuf, slot, pair, ie, pair != cur_pair, zres, status, gout, r1out, r2out,
+                      item * p.n_gauge);
         cur_pair = pair;
     }
 }

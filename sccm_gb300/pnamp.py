@@ -33,6 +33,7 @@ ST_PIVOT_UNDERFLOW = 1
 ST_SINGULAR_T22 = 2
 ST_NONFINITE = 4
 ST_SINGULAR_U = 8
+ST_CONTRACTION = 16
 
 NK = 2 * JJMAX + 1
 FIELDS = ("njkk", "hjkk", "nn", "zz", "J2")
@@ -49,8 +50,10 @@ EXPORTS = ("pnamp_init", "pnamp_n_euler", "pnamp_pair", "pnamp_batch", "pnamp_ba
            "pnamp_set_outputs", "pnamp_batch_items_device", "pnamp_rho1b_blocks", "pnamp_batch_rho1b_device",
            "pnamp_batch_rho1b", "pnamp_project_rho1b", "pnamp_rho2b_layout", "pnamp_rho2b_tables",
            "pnamp_batch_rho2b_device", "pnamp_batch_rho2b", "pnamp_project_rho2b",
-           "pnamp_batch_densities_device", "pnamp_batch_densities")
-FORMS = {"fp64": 0, "df64": 1}
+           "pnamp_batch_densities_device", "pnamp_batch_densities", "pnamp_set_timing", "pnamp_stage_times")
+# arithmetic forms (include/pnamp_gpu.h PNAMP_FORM_*): plain FP64, double-float per-point algebra,
+# and the latter with the two-body contraction on the tensor cores as BF16x3 or BF16x6
+FORMS = {"fp64": 0, "df64": 1, "tc3": 2, "tc6": 3}
 PNAMP_ERR_SCRATCH_LIMIT = 7
 PNAMP_ERR_SMALL_NORM = 8
 
@@ -139,6 +142,8 @@ def load_library(path: str | None = None):
     lib.pnamp_multi_free.argtypes = [vp]
     lib.pnamp_multi_free.restype = None
     lib.pnamp_sync.argtypes = [vp]
+    lib.pnamp_set_timing.argtypes = [vp, C.c_int]
+    lib.pnamp_stage_times.argtypes = [vp, vp]
     lib.pnamp_free.argtypes = [vp]
     lib.pnamp_free.restype = None
     lib.pnamp_strerror.argtypes = [C.c_int]
@@ -194,6 +199,43 @@ def rho2b_tables(sp: ModelSpace):
     return {"blocks": blocks, "quads": q4, "ptr": ptr, "term_q": tq, "term_c": tc}
 
 
+def abi_structs(sp: ModelSpace, e0: float, t1b, recs, vbar, mesh: Mesh, q2=None, cscale: float = 1.0,
+                iscale: int = 0):
+    """The pnamp_space / pnamp_hamiltonian / pnamp_mesh structs of include/pnamp_gpu.h for these
+    inputs, and the arrays they point into (keep them alive while the structs are used)."""
+    n = sp.nlev
+    keep = []
+
+    def ia(x):
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.int32))
+        keep.append(a)
+        return a
+
+    def da(x):
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
+        keep.append(a)
+        return a
+
+    space = _Space(n, sp.nprot, sp.nneut, sp.core_prot, sp.core_neut,
+                   _iptr(ia(sp.t)), _iptr(ia(sp.n)), _iptr(ia(sp.l)),
+                   _iptr(ia(sp.twoj)), _iptr(ia(sp.twom)))
+    recs = np.asarray(recs, dtype=np.int32).reshape(-1, 4)
+    t1 = da(np.real(np.asarray(t1b)).T)        # column-major
+    q = None
+    if q2 is not None:
+        q = da(np.asarray(q2, dtype=np.float64).transpose(0, 2, 1))   # each block column-major
+    ham = _Ham(float(e0), _dptr(t1), int(recs.shape[0]),
+               _iptr(ia(recs[:, 0] + 1)), _iptr(ia(recs[:, 1] + 1)),
+               _iptr(ia(recs[:, 2] + 1)), _iptr(ia(recs[:, 3] + 1)),
+               _dptr(da(vbar)), _dptr(q) if q is not None else None)
+    msh = _Mesh(mesh.nalp, mesh.nbet, mesh.ngam, mesh.nfom, mesh.ncosbet,
+                _dptr(da(mesh.alpha)), _dptr(da(mesh.walp)),
+                _dptr(da(mesh.beta)), _dptr(da(mesh.wbet)),
+                _dptr(da(mesh.gamma)), _dptr(da(mesh.wgam)),
+                float(cscale), int(iscale))
+    return space, ham, msh, keep
+
+
 class PnampContext:
     """A built PNAMP context: model space + Hamiltonian + mesh on the GPU."""
 
@@ -202,35 +244,7 @@ class PnampContext:
         lib = load_library()
         n = sp.nlev
         self.sp, self.mesh, self.n = sp, mesh, n
-        keep = []
-
-        def ia(x):
-            a = np.ascontiguousarray(np.asarray(x, dtype=np.int32))
-            keep.append(a)
-            return a
-
-        def da(x):
-            a = np.ascontiguousarray(np.asarray(x, dtype=np.float64))
-            keep.append(a)
-            return a
-
-        self._space = _Space(n, sp.nprot, sp.nneut, sp.core_prot, sp.core_neut,
-                             _iptr(ia(sp.t)), _iptr(ia(sp.n)), _iptr(ia(sp.l)),
-                             _iptr(ia(sp.twoj)), _iptr(ia(sp.twom)))
-        recs = np.asarray(recs, dtype=np.int32).reshape(-1, 4)
-        t1 = da(np.real(np.asarray(t1b)).T)        # column-major
-        q = None
-        if q2 is not None:
-            q = da(np.asarray(q2, dtype=np.float64).transpose(0, 2, 1))   # each block column-major
-        self._ham = _Ham(float(e0), _dptr(t1), int(recs.shape[0]),
-                         _iptr(ia(recs[:, 0] + 1)), _iptr(ia(recs[:, 1] + 1)),
-                         _iptr(ia(recs[:, 2] + 1)), _iptr(ia(recs[:, 3] + 1)),
-                         _dptr(da(vbar)), _dptr(q) if q is not None else None)
-        self._mesh = _Mesh(mesh.nalp, mesh.nbet, mesh.ngam, mesh.nfom, mesh.ncosbet,
-                           _dptr(da(mesh.alpha)), _dptr(da(mesh.walp)),
-                           _dptr(da(mesh.beta)), _dptr(da(mesh.wbet)),
-                           _dptr(da(mesh.gamma)), _dptr(da(mesh.wgam)),
-                           float(cscale), int(iscale))
+        self._space, self._ham, self._mesh, keep = abi_structs(sp, e0, t1b, recs, vbar, mesh, q2, cscale, iscale)
         self._keep = keep
         h = C.c_void_p()
         rc = lib.pnamp_init(C.byref(self._space), C.byref(self._ham), C.byref(self._mesh), C.byref(h))
@@ -241,7 +255,8 @@ class PnampContext:
         self.set_form(form)
 
     def set_form(self, form: str):
-        """Arithmetic of the per-point algebra: "fp64" (plain) or "df64" (double-float)."""
+        """Arithmetic form: "fp64" (plain), "df64" (double-float per-point algebra), "tc3" / "tc6"
+        (double-float with the two-body contraction on the tensor cores, BF16x3 / BF16x6)."""
         rc = load_library().pnamp_set_form(self._h, FORMS[form])
         if rc != PNAMP_OK:
             raise PnampError(rc, "pnamp_set_form")
@@ -462,6 +477,22 @@ class PnampContext:
         rc = load_library().pnamp_sync(self._h)
         if rc != PNAMP_OK:
             raise PnampError(rc, "pnamp_sync")
+
+    def set_timing(self, on=True):
+        """Record CUDA events around the launches of later batch calls (pnamp_set_timing)."""
+        rc = load_library().pnamp_set_timing(self._h, 1 if on else 0)
+        if rc != PNAMP_OK:
+            raise PnampError(rc, "pnamp_set_timing")
+
+    def stage_times(self):
+        """ms of the last batch call's stages: dict(setup, points, contract, finish)."""
+        ms = np.zeros(4)
+        rc = load_library().pnamp_stage_times(self._h, ms.ctypes.data)
+        if rc < 0 or rc > 4 and rc != 4:
+            raise PnampError(rc, "pnamp_stage_times")
+        if rc != 4:
+            raise PnampError(rc, "pnamp_stage_times")
+        return dict(zip(("setup", "points", "contract", "finish"), ms.tolist()))
 
 
 class MultiPlan:
