@@ -160,7 +160,19 @@ contract_kernel(const __grid_constant__ TcMaps maps, TcArgs a) {
                         }
                     }
             }
-        // the ring's copies must land before the CTA can leave
+        // the tensor core's last arrivals on the ring's empty barriers (one per stage in use)
+        // must land before the CTA leaves: wait for each stage as if it were to be refilled
+        for (int t = 0; t < kTcStages && ok; ++t) {
+            if (!tc::mbar_wait(&empty[s], ph ^ 1u, abort, kWaitNs)) {
+                fail(1);
+                ok = false;
+            }
+            if (++s == kTcStages) {
+                s = 0;
+                ph ^= 1u;
+            }
+        }
+        // and the ring's copies must land before the CTA can leave
         volatile int never = 0;
         for (int t = 0; t < kTcStages; ++t)
             if (issued[t] && !tc::mbar_wait(&full[t], issued_par[t], &never, kWaitNs)) atomicOr(a.err, 8);

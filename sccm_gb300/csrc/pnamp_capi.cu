@@ -73,6 +73,7 @@ struct pnamp_ctx {
     double *d_tc_w = nullptr, *d_tc_e2 = nullptr;
     int *d_tc_err = nullptr;
     long long tc_cap_pts = 0;
+    int tc_cap_splits = 0;                       // bf16 terms the staging was allocated for
     int nsm = 0;
     // per-stage CUDA-event timing of the last pnamp_batch_device / items call (pnamp_set_timing)
     int timing = 0;
@@ -512,7 +513,9 @@ int build_tc(pnamp_ctx *c) {
 
 // Staging for `pts` kernel points: X and Y rows per bf16 term, weights, E2.
 int ensure_tc_staging(pnamp_ctx *c, long long pts) {
-    if (pts <= c->tc_cap_pts) return PNAMP_OK;
+    // a form switch from BF16x3 to BF16x6 needs the third term's arrays too
+    if (pts <= c->tc_cap_pts && c->tc_splits <= c->tc_cap_splits) return PNAMP_OK;
+    pts = std::max(pts, c->tc_cap_pts);
     for (int sp = 0; sp < 3; ++sp) {
         if (c->d_tc_x[sp]) cudaFree(c->d_tc_x[sp]);
         if (c->d_tc_y[sp]) cudaFree(c->d_tc_y[sp]);
@@ -522,6 +525,7 @@ int ensure_tc_staging(pnamp_ctx *c, long long pts) {
     if (c->d_tc_e2) cudaFree(c->d_tc_e2);
     c->d_tc_w = c->d_tc_e2 = nullptr;
     c->tc_cap_pts = 0;
+    c->tc_cap_splits = 0;
     const int npp = c->tc_nk - c->tc_nph;
     for (int sp = 0; sp < c->tc_splits; ++sp) {
         CK(cudaMalloc(&c->d_tc_x[sp], (size_t)pts * 2 * c->tc_nk * sizeof(uint16_t)));
@@ -530,6 +534,7 @@ int ensure_tc_staging(pnamp_ctx *c, long long pts) {
     CK(cudaMalloc(&c->d_tc_w, (size_t)pts * 2 * sizeof(double)));
     CK(cudaMalloc(&c->d_tc_e2, (size_t)pts * 2 * sizeof(double)));
     c->tc_cap_pts = pts;
+    c->tc_cap_splits = c->tc_splits;
     return PNAMP_OK;
 }
 
@@ -560,6 +565,9 @@ int tc_run(pnamp_ctx *c, int npairs, const double *d_uv, double *d_zres, int *d_
     const long long chunk_pts =
         std::min<long long>(tc_chunk_points(c, items ? (long long)G : (long long)P * G), total_items * G);
     if ((rc = ensure_tc_staging(c, chunk_pts)) != PNAMP_OK) return rc;
+    for (int sp = 0; sp < c->tc_splits; ++sp)   // every term the kernels write and read must exist
+        if (!c->d_tc_x[sp] || !c->d_tc_y[sp] || !c->d_tc_mat[sp]) return PNAMP_ERR_STATE;
+    if (!c->d_tc_w || !c->d_tc_e2 || chunk_pts > c->tc_cap_pts) return PNAMP_ERR_STATE;
     const long long chunk_items = chunk_pts / G;
     Params q = c->p;
     q.tc_splits = c->tc_splits;

@@ -8,7 +8,9 @@ levels and of each vacuum's K-mixed E_J, in keV. The plain FP64 path is itself
 pinned to the FP64 oracle at 1e-10 (tests/test_gpu_parity.py), so these are
 the form's errors against the oracle up to that bound.
 
-    python -m sccm_gb300.forms --workload pf --nvac 20 --mesh 10,20,10,9 --form df64
+    python -m sccm_gb300.forms --workload pf --nvac 20 --mesh 10,20,10,9 --form df64,tc3,tc6 [--pn-mix]
+
+Several forms are compared against one FP64 run; one JSON line per form.
 """
 from __future__ import annotations
 
@@ -38,8 +40,8 @@ def run_form(wl, form, batch=8):
     return zs, kerns, dt
 
 
-def compare(wl, form, ref_form="fp64", batch=8):
-    za, ka, ta = run_form(wl, ref_form, batch)
+def compare(wl, form, ref_form="fp64", batch=8, ref=None):
+    za, ka, ta = ref if ref is not None else run_form(wl, ref_form, batch)
     zb, kb, tb = run_form(wl, form, batch)
     rel_n = max(float(np.abs(b[:, 0] - a[:, 0]).max() / np.abs(a[:, 0]).max()) for a, b in zip(za, zb))
     rel_h = max(float(np.abs(b[:, 6] - a[:, 6]).max() / np.abs(a[:, 6]).max()) for a, b in zip(za, zb))
@@ -62,10 +64,16 @@ def main():
     ap.add_argument("--nvac", type=int, default=20)
     ap.add_argument("--mesh", default="10,20,10,9")
     ap.add_argument("--seed", type=int, default=2000)
-    ap.add_argument("--form", default="df64")
+    ap.add_argument("--form", default="df64", help="comma-separated forms to compare with FP64")
+    ap.add_argument("--pn-mix", action="store_true", help="vacua that mix protons and neutrons (general path)")
     args = ap.parse_args()
-    wl = make_workload(args.workload, args.nvac, Mesh(*[int(x) for x in args.mesh.split(",")]), seed=args.seed)
-    print(json.dumps(compare(wl, args.form)))
+    wl = make_workload(args.workload, args.nvac, Mesh(*[int(x) for x in args.mesh.split(",")]), seed=args.seed,
+                       pn_mix=args.pn_mix)
+    ref = run_form(wl, "fp64")
+    for form in args.form.split(","):
+        r = compare(wl, form, ref=ref)
+        r["pn_mix"] = bool(args.pn_mix)
+        print(json.dumps(r), flush=True)
 
 
 if __name__ == "__main__":

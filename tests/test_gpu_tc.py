@@ -136,3 +136,21 @@ def test_items_path_matches_full_mesh(pf):
     assert np.allclose(zi[idx], full[idx], rtol=0, atol=1e-12 * np.abs(full).max())
     others = np.setdiff1d(np.arange(P), idx)
     assert np.abs(zi[others]).max() == 0.0
+
+
+def test_form_switches_on_one_context(pf):
+    """BF16x3 -> BF16x6 -> BF16x3 -> double-float on one context: the staging grows to the
+    third bf16 term when BF16x6 follows BF16x3, and each form gives its own result."""
+    pairs = [(*pf.vacua[0], *pf.vacua[1])]
+    got = {}
+    with ctx_for(pf, "tc3") as ctx:
+        for form in ("tc3", "tc6", "tc3", "df64"):
+            ctx.set_form(form)
+            z, st = ctx.batch(pairs)
+            assert not (st & ST_CONTRACTION).any()
+            got.setdefault(form, []).append(z[0])
+    ref = got["df64"][0]
+    for form in ("tc3", "tc6"):
+        for z in got[form]:
+            assert_tc_close(z, ref, form)
+    assert np.array_equal(got["tc3"][0], got["tc3"][1])
