@@ -1,29 +1,32 @@
 #!/usr/bin/env python3
 """Benchmark of the GB300 PNAMP kernel path: projected kernel points/s.
 
-Workload (the configuration the metric is quoted on that fits one GPU):
-pf shell (0f7/2, 1p3/2, 0f5/2, 1p1/2; n = 40 m-states), 4 + 4 valence
-nucleons, 20 seeded quadrupole-deformed HFB vacua (beta2 in [0, 0.5], gamma in
-[0, 60] deg) giving 210 symmetric (q, q') pairs, Euler mesh 10 x 20 x 10 with
-9 x 9 gauge points (162,000 kernel points per pair), seeded random J-coupled
-isospin-symmetric TBMEs. A kernel point is one (q, q', alpha, beta, gamma,
-phi_n, phi_p) evaluation. One step = `--pairs-per-step` pairs through the full
-per-pair path (setup, mesh loop, J/K projection); steps walk round robin over
-the pair list. For N > 1 (torchrun), pairs are dealt to ranks as in the
-reference's MPI round robin (rank == ic mod nprocs): weak scaling, no
-collective on the data path.
+Workload (the configuration the metric is quoted on that fits one GPU): pf shell
+(0f7/2, 1p3/2, 0f5/2, 1p1/2; n = 40 m-states), 4 + 4 valence nucleons, 20 seeded
+quadrupole-deformed HFB vacua (beta2 in [0, 0.5], gamma in [0, 60] deg) giving 210
+symmetric (q, q') pairs, Euler mesh 10 x 20 x 10 with 9 x 9 gauge points (162,000 kernel
+points per pair), seeded random J-coupled isospin-symmetric TBMEs. A kernel point is one
+(q, q', alpha, beta, gamma, phi_n, phi_p) evaluation. These vacua conserve charge, so the
+kernels take their species-split path; beside the headline the same run times the general
+path on the same set with proton-neutron mixing vacua, and the reference's own Ti48 / KB3G
+vacua and interaction (proton-neutron pairing, general path) on the same mesh. One step =
+`--pairs-per-step` pairs through setup, mesh loop (and, in the tensor-core forms, the
+contraction) and J/K projection; steps walk round robin over the pair list. For N > 1
+(torchrun), pairs are dealt to ranks as in the reference's MPI round robin (rank == ic mod
+nprocs): weak scaling, no collective on the data path.
 
-`value`: device-resident inputs (uploaded before timing), CUDA-event time of
-the steps on the launching stream, L2 flushed (256 MiB write) before each step
-outside its events.  `e2e`: the same steps through the host-buffer C ABI
-(`pnamp_batch` + `pnamp_project`) from pinned host memory, results read back.
-`--impl reference`: the CPU oracle port (the reference Fortran cannot be
-compiled here), all host cores, bounded samples of the same workload.
+`value`: device-resident inputs (uploaded before timing), CUDA-event time of the steps on
+the launching stream, L2 flushed (256 MiB write) before each step outside its events.
+`e2e`: the same steps through the host-buffer C ABI (`pnamp_batch` + `pnamp_project`) from
+pinned host memory, results read back. Per-kernel times for the rooflines come from the
+library's own CUDA events around its launches (`pnamp_set_timing`). `--impl reference`: the
+C++/OpenMP restatement of the reference's CPU path (oracle/cpu; the reference Fortran cannot
+be compiled here), all host cores, bounded samples of the same steps' pairs.
 
-Other workloads (their own JSON lines, not the headline): `--workload uneven`
-(three model spaces and meshes in persistent launches and one CUDA graph),
-`--workload learned` (the learned mode against the exact mixed form on a fine
-mesh), `--workload rho2b` (the pf set with the two-body transition density).
+Other workloads (their own JSON lines, not the headline): `--workload uneven` (three model
+spaces and meshes in persistent launches and one CUDA graph), `--workload learned` (the
+learned mode against the exact mixed form on a fine mesh), `--workload rho2b` (the pf set
+with the two-body transition density).
 """
 from __future__ import annotations
 
@@ -42,44 +45,82 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "projected kernel points/s on 1 GB300: learned+mixed vs plain FP64 at <=1 keV E_J"
-WORKLOAD = ("pf shell n=40 (Z=4, N=4 valence), 20 seeded deformed vacua -> 210 pairs, "
-            "Euler 10x20x10 x gauge 9x9 = 162000 points/pair")
+WORKLOAD = ("pf shell n=40 (Z=4, N=4 valence), 20 seeded deformed charge-conserving vacua -> 210 pairs, "
+            "Euler 10x20x10 x gauge 9x9 = 162000 points/pair (species-split path)")
 FORM_TEXT = {"fp64": "plain FP64",
              "df64": "mixed: per-point algebra in double-float (FP32 pairs) on the FP32 pipes, FP64 "
-                     "preparation and reductions; norm kernel within 1e-10 of FP64"}
-# DRAM bytes per kernel point of the FP64 point kernel (ncu dram__bytes_read + write on a
-# 20,736-point launch of this workload, scaled by points): all per-point matrices live in
-# shared memory or an L2-resident slot, so traffic is tiny.
-TRAFFIC_BYTES_PER_POINT = (553984.0 + 2560.0) / 20736.0
+                     "preparation and reductions",
+             "tc3": "mixed, with the two-body contraction as block GEMMs on the tcgen05 tensor cores in "
+                    "BF16x3 (two bf16 terms per value, three products, FP32 accumulation)",
+             "tc6": "mixed, with the two-body contraction as block GEMMs on the tcgen05 tensor cores in "
+                    "BF16x6 (three bf16 terms per value, six products, FP32 accumulation)"}
+FORMS = ("fp64", "df64", "tc3", "tc6")
+# Double-float cost: a complex multiply-add (8 FP64-equivalent flops) is four double-float
+# FMAs of 15 FP32 instructions each (pnamp_df64.cuh: one multiply, three FMAs, TwoSum's six
+# additions, three additions, FastTwoSum's two), i.e. 7.5 FP32 instructions per flop.
+FP32_INSTR_PER_FLOP = 7.5
+# DRAM bytes per kernel point of the point kernels (ncu dram__bytes_read + write on launches of
+# this workload, scaled by points): all per-point matrices live in shared memory or an
+# L2-resident slot, so traffic is tiny.
+TRAFFIC_BYTES_PER_POINT = {"fp64": (553984.0 + 2560.0) / 20736.0, "df64": 43.0}
 
 
-def algorithmic_flops_per_point(wl, n_gauge):
-    """Algorithmic FP64 work per kernel point: the minimal flops of the algorithm the
-    kernel runs (complex multiply-add = 8 flops, complex x real = 4), O(n^2) terms left out.
+def _pair_paths(wl, pairs):
+    """(species-split, reduced Pfaffian) per pair, as the set-up kernel decides them: split
+    when the four matrices have no proton-neutron blocks, reduced when V0's LU pivots span
+    less than 1e2."""
+    import scipy.linalg as sl
+    n = wl.sp.nlev
+    h = n // 2
+    out = []
+    for i, j in pairs:
+        (U0, V0), (U1, V1) = wl.vacua[i], wl.vacua[j]
+        split = all(not np.any(np.asarray(M)[:h, h:]) and not np.any(np.asarray(M)[h:, :h])
+                    for M in (U0, V0, U1, V1))
+        d = np.abs(np.diag(sl.lu_factor(V0)[0]))
+        reduced = bool(d.min() >= 1e-2 * d.max())
+        out.append((split and reduced, reduced))
+    return out
+
+
+def algorithmic_flops_per_point(wl, n_gauge, pairs=None, records=True):
+    """Algorithmic FP64 work per kernel point of the point kernel, averaged over `pairs`
+    (default: all): the minimal flops of the algorithm it runs (complex multiply-add = 8
+    flops, complex x real = 4), O(n^2) terms left out.
 
     Per Euler point, amortised over the n_gauge gauge points: R W, R V1, conj(R) U1 and
     X = (R W) R^T with the block-diagonal rotation, (3 * 4 + 8) n sum_b d_b^2, and the
     four T22 partials (n x n x h, complex x real), 8 n^3.
-    Per point: the Pfaffian of the n x n Schur complement c (D X D - Z0^-1), (4/3) n^3;
-    Y T22^-1 for the 2n x n right-hand sides counted as LU + solves, (8/3 + 16) n^3;
-    the density products, 12 n^3. For a species-split pair (charge-conserving vacua:
-    no proton-neutron blocks) these run on two h x h blocks, h = n/2: a quarter.
-    Two-body records: 52 flops (28 when i + j = k + l, which halves the terms); for a
-    split pair the proton-neutron records keep two of the four density products, 18 (10).
+    Per point: the Pfaffian of the n x n Schur complement c (D X D - Z0^-1), (4/3) n^3, or of
+    the 2n x 2n matrix, (4/3) (2n)^3, when V0 is ill conditioned; Y T22^-1 for the 2n x n
+    right-hand sides counted as LU + solves, (8/3 + 16) n^3; the density products, 12 n^3.
+    For a species-split pair these run on two h x h blocks, h = n/2: a quarter.
+    Two-body records (`records`; the tensor-core forms contract them in their own kernel):
+    52 flops (28 when i + j = k + l, which halves the terms); for a split pair the proton-
+    neutron records keep two of the four density products, 18 (10).
     """
     n = wl.sp.nlev
     h = n // 2
     sd2 = sum(d * d for _, d in wl.sp.blocks())
-    split = all(not np.any(np.asarray(M)[:h, h:]) and not np.any(np.asarray(M)[h:, :h])
-                for U, V in wl.vacua for M in (U, V))
     r = np.asarray(wl.recs)
     i, j, k, l = r.T
-    pn = (i < h) & (j >= h) & (k < h) & (l >= h) if split else np.zeros(len(r), bool)
+    pn = (i < h) & (j >= h) & (k < h) & (l >= h)
     diag = (i + j) == (k + l)
-    rec = (52.0 * np.sum(~pn & ~diag) + 28.0 * np.sum(~pn & diag)
-           + 18.0 * np.sum(pn & ~diag) + 10.0 * np.sum(pn & diag))
-    dense = (4.0 / 3.0 + 8.0 / 3.0 + 16.0 + 12.0) * n ** 3 * (0.25 if split else 1.0)
-    return (20.0 * n * sd2 + 8.0 * n ** 3) / n_gauge + dense + float(rec)
+    tot = 0.0
+    paths = _pair_paths(wl, pairs if pairs is not None else wl.pairs)
+    for split, reduced in paths:
+        pfaff = (4.0 / 3.0) * (n if reduced else 2 * n) ** 3
+        dense = (pfaff + (8.0 / 3.0 + 16.0 + 12.0) * n ** 3) * (0.25 if split else 1.0)
+        if records:
+            if split:
+                rec = (52.0 * np.sum(~pn & ~diag) + 28.0 * np.sum(~pn & diag)
+                       + 18.0 * np.sum(pn & ~diag) + 10.0 * np.sum(pn & diag))
+            else:
+                rec = 52.0 * np.sum(~diag) + 28.0 * np.sum(diag)
+        else:
+            rec = 0.0
+        tot += (20.0 * n * sd2 + 8.0 * n ** 3) / n_gauge + dense + float(rec)
+    return tot / len(paths)
 
 
 SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -87,32 +128,30 @@ SMI_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.act
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
 
-# ------------------------------------------------------------------ CPU oracle
-def _oracle_task(args):
-    sp, ham, mesh, U0, V0, U1, V1, ie = args
-    from oracle.pnamp_oracle import kernel_triaxial
-    z = kernel_triaxial(sp, ham, mesh, U0, V0, U1, V1, euler_subset=[ie])
-    return z[ie]
-
-
-def cpu_sample(pool, ncores, wl, n_euler_sample, pair_index=0):
-    """Oracle port on `n_euler_sample` Euler points x all gauge points of one pair."""
-    from oracle.pnamp_oracle import Hamiltonian
-    ham = Hamiltonian(wl.e0, wl.t1b, wl.recs, wl.vbar, wl.q2, wl.jops)
-    i, j = wl.pairs[pair_index]
-    (U0, V0), (U1, V1) = wl.vacua[i], wl.vacua[j]
+# ------------------------------------------------------------------ CPU baseline
+def cpu_rate(wl, pairs, n_euler_sample, form="minimal", threads=0, seed=0):
+    """The C++/OpenMP restatement (oracle/cpu) on a sample of Euler points x all gauge points
+    spread over `pairs`; returns (points/s, seconds, points)."""
+    from oracle import cpu_baseline as cb
+    rng = np.random.default_rng(seed)
     P = wl.mesh.n_euler
-    tasks = [(wl.sp, ham, wl.mesh, U0, V0, U1, V1, (k * 7919) % P) for k in range(n_euler_sample)]
-    t0 = time.perf_counter()
-    pool.map(_oracle_task, tasks, chunksize=1)
-    dt = time.perf_counter() - t0
-    return n_euler_sample * wl.mesh.n_gauge / dt, dt
+    per = max(1, n_euler_sample // len(pairs))
+    t = 0.0
+    pts = 0
+    for (i, j) in pairs:
+        idx = np.sort(rng.choice(P, size=min(per, P), replace=False))
+        t0 = time.perf_counter()
+        cb.zres(wl, wl.mesh, i, j, form, euler=idx, threads=threads)
+        t += time.perf_counter() - t0
+        pts += len(idx) * wl.mesh.n_gauge
+    return pts / t, t, pts
 
 
-def make_pool(ncores):
-    os.environ.setdefault("OMP_NUM_THREADS", "1")
-    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
-    return mp.get_context("spawn").Pool(ncores)
+def cpu_calibrated(wl, pairs, seconds, form="minimal", threads=0):
+    """cpu_rate on a sample sized to take about `seconds`."""
+    r0, t0, p0 = cpu_rate(wl, pairs, 4 * len(pairs), form, threads, seed=1)
+    n = int(max(len(pairs), 4 * len(pairs) * seconds / max(t0, 1e-3)))
+    return cpu_rate(wl, pairs, n, form, threads, seed=2)
 
 
 # ------------------------------------------------------------------ clocks
@@ -170,10 +209,11 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ main
-def fp64_peak_tflops(torch):
-    """cuBLAS DGEMM 4096^3, best of 5, CUDA events: the FP64 pipe ceiling on this GPU."""
-    a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
-    b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+def gemm_peak_tflops(torch, dtype, size=4096):
+    """cuBLAS GEMM size^3, best of 5, CUDA events: the pipe ceiling of `dtype` on this GPU
+    (FP64 for the plain form, FP32 for the double-float form's instruction issue)."""
+    a = torch.randn(size, size, dtype=dtype, device="cuda")
+    b = torch.randn(size, size, dtype=dtype, device="cuda")
     for _ in range(2):
         a @ b
     best = 1e30
@@ -184,7 +224,16 @@ def fp64_peak_tflops(torch):
         e.record()
         torch.cuda.synchronize()
         best = min(best, s.elapsed_time(e) / 1e3)
-    return 2 * 4096 ** 3 / best / 1e12
+    return 2 * size ** 3 / best / 1e12
+
+
+def measured_peaks():
+    """MEASURED_PEAKS.json next to this file (HBM GB/s, bf16 TFLOP/s burst and sustained)."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
 
 
 UNEVEN_WORKLOAD = ("uneven batch: 64 sd pairs (n=24, Euler 8x16x8, gauge 7x7), 128 pf pairs (n=40, "
@@ -367,9 +416,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--form", default="df64", choices=["fp64", "df64"],
-                    help="arithmetic of the per-point algebra: plain FP64 or double-float")
-    ap.add_argument("--no-compare", action="store_true", help="skip timing the plain FP64 form as well")
+    ap.add_argument("--form", default="df64", choices=list(FORMS),
+                    help="headline arithmetic form: plain FP64, double-float, or double-float with the "
+                         "two-body contraction on the tensor cores (BF16x3, BF16x6)")
+    ap.add_argument("--compare-forms", default=None,
+                    help="comma-separated forms timed beside the headline on the same pairs (default: all)")
+    ap.add_argument("--no-general", action="store_true",
+                    help="skip the general-path workloads (pn-mixing vacua, Ti48/KB3G)")
+    ap.add_argument("--secondary-steps", type=int, default=3, help="timed steps of the general-path workloads")
     ap.add_argument("--mesh", default=None,
                     help="override the mesh as NALP,NBET,NGAM,NFOM (small cases for profiling captures)")
     ap.add_argument("--workload", default="pf", choices=["pf", "uneven", "learned", "rho2b"],
@@ -398,46 +452,52 @@ def main():
     ncores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
 
     from sccm_gb300.basis import Mesh
-    from sccm_gb300.synth import config
+    from sccm_gb300.driver import rank_pairs
+    from sccm_gb300.synth import config, ti48_workload
     wl = config(1)
     if args.mesh:
         wl.mesh = Mesh(*[int(x) for x in args.mesh.split(",")])
+    pps = args.pairs_per_step
+    mine = rank_pairs(wl.pairs, rank, world)
+    order = [mine[k % len(mine)] for k in range((args.warmup + args.steps) * pps)]
+    line_config = {"workload": WORKLOAD, "form": FORM_TEXT[args.form], "pairs_per_step": pps,
+                   "points_per_pair": wl.mesh.n_euler * wl.mesh.n_gauge,
+                   "l2": "flushed (256 MiB write) before each step",
+                   "parallelism": f"pairs round-robin over {world} rank(s)"}
 
     if args.impl == "reference":
         if rank != 0:
             return 0
-        pool = make_pool(ncores)
-        # bounded sample per step: ~ncores Euler points x all gauge points of pair 0
-        rate, dt = cpu_sample(pool, ncores, wl, ncores)          # calibration / warm-up
-        nsamp = max(ncores, int(ncores * max(1.0, 8.0 / max(dt, 1e-3))))
-        for _ in range(max(0, args.warmup - 1)):
-            cpu_sample(pool, ncores, wl, nsamp)
-        tot_pts, tot_t = 0, 0.0
-        for _ in range(args.steps):
-            r, t = cpu_sample(pool, ncores, wl, nsamp)
-            tot_pts += r * t
+        # the C++/OpenMP CPU restatement on every host core, each step a bounded sample of
+        # Euler points (all gauge points) of that step's pairs
+        from oracle import cpu_baseline as cb
+        cb.build()
+        nth = cb.max_threads()
+        first = order[:pps]
+        _, t0, _ = cpu_rate(wl, first, 2 * pps)
+        per_step = int(max(pps, 2 * pps * args.cpu_seconds / 5.0 / max(t0, 1e-3)))
+        for k in range(args.warmup):
+            cpu_rate(wl, order[k * pps:(k + 1) * pps], pps, seed=k)
+        tot_t = tot_p = 0.0
+        for k in range(args.steps):
+            r, t, p = cpu_rate(wl, order[(args.warmup + k) * pps:(args.warmup + k + 1) * pps], per_step,
+                               seed=100 + k)
             tot_t += t
-        pool.close()
-        v = tot_pts / tot_t
-        sample = f"{nsamp} Euler points x 81 gauge points of pair (0,0) per step"
+            tot_p += p
+        v = tot_p / tot_t
+        sample = (f"{per_step} Euler points x {wl.mesh.n_gauge} gauge points per step, spread over the step's "
+                  f"{pps} pairs; oracle/cpu/pnamp_cpu.cpp, minimal form, {nth} OpenMP threads")
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": v, "unit": "points/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD},
-            "cpu_baseline": {"value": v, "unit": "points/s", "cores": ncores, "kind": "port",
-                             "sample": sample},
+            "data": "synthetic: seeded vacua and TBMEs (no public dataset exists)", "config": line_config,
+            "cpu_baseline": {"value": v, "unit": "points/s", "cores": nth, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return 0
 
-    # CPU baseline pool before any GPU call (spawned workers never touch CUDA)
-    pool = None
-    if not args.no_cpu_baseline and rank == 0 and world == 1:
-        pool = make_pool(ncores)
-
-    import numpy as np
     import torch
-    from sccm_gb300.driver import rank_pairs
+    from sccm_gb300.contraction import gemm_flops_per_point
     from sccm_gb300.pnamp import PnampContext
 
     torch.cuda.set_device(local_rank)
@@ -445,87 +505,89 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-
-    ctx = PnampContext(wl.sp, wl.e0, wl.t1b, wl.recs, wl.vbar, wl.mesh, q2=wl.q2)
-    P = ctx.n_euler
-    G = wl.mesh.n_gauge
-    pts_per_pair = P * G
-    mine = rank_pairs(wl.pairs, rank, world)
-    pps = args.pairs_per_step
-    nsteps_total = args.warmup + args.steps
-    order = [mine[(k) % len(mine)] for k in range(nsteps_total * pps)]
-    quads = [(*wl.vacua[i], *wl.vacua[j]) for (i, j) in order]
-    packed = PnampContext.pack_pairs(quads)                           # [npairs, 4, n, n]
-    stream = torch.cuda.Stream()
     dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
     fs = 5 * 7 * 13 * 13 * 2
     with torch.cuda.stream(stream):
-        d_uv = torch.from_numpy(packed).to(dev)
-        d_z = torch.zeros((pps, 19 * P * 2), dtype=torch.float64, device=dev)
-        d_st = torch.zeros((pps, P), dtype=torch.int32, device=dev)
-        d_proj = torch.zeros((pps, fs), dtype=torch.float64, device=dev)
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    sh = stream.cuda_stream
-    per_pair_uv = packed[0].nbytes
 
-    def step(k, ev=None):
-        off = d_uv.data_ptr() + k * pps * per_pair_uv
-        if ev:
-            ev[0].record(stream)
-        ctx.batch_device(pps, off, d_z.data_ptr(), d_st.data_ptr(), sh)
-        if ev:
-            ev[1].record(stream)
-        ctx.project_device(pps, d_z.data_ptr(), d_proj.data_ptr(), True, sh)
-        if ev:
-            ev[2].record(stream)
-
-    def timed(form):
-        """W untimed + K timed steps of one arithmetic form; (total s, point-kernel ms list, clocks)."""
-        ctx.set_form(form)
+    def timed_forms(w, ctx, pair_order, forms, steps, warmup, tag):
+        """W untimed + K timed steps per form on device-resident inputs; per form: total s,
+        stage ms (library events), clocks, status."""
+        P = ctx.n_euler
+        packed = PnampContext.pack_pairs([(*w.vacua[i], *w.vacua[j]) for (i, j) in pair_order])
+        per_pair_uv = packed[0].nbytes
         with torch.cuda.stream(stream):
-            for k in range(args.warmup):
-                flush.zero_()
-                step(k)
-            torch.cuda.synchronize()
-            if dist:
-                dist.barrier()
-            evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-            with ClockSampler(clock_path(args, f"{form}_rank{rank}")) as clk:
-                torch.cuda.synchronize()
-                for k in range(args.steps):
-                    flush.zero_()
-                    step(args.warmup + k, evs[k])
-                torch.cuda.synchronize()
-            if dist:
-                dist.barrier()
-        step_ms = [e[0].elapsed_time(e[2]) for e in evs]
-        tot = sum(step_ms) / 1e3
-        if dist:
-            t = torch.tensor([tot], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tot = float(t)
-        status = d_st.cpu().numpy()
-        if (status & ~1).any():
-            raise RuntimeError(f"non-trivial point status flags ({form}): {np.unique(status)}")
-        return tot, [e[0].elapsed_time(e[1]) for e in evs], clk.summary(local_rank)
+            d_uv = torch.from_numpy(packed).to(dev)
+            d_z = torch.zeros((pps, 19 * P * 2), dtype=torch.float64, device=dev)
+            d_st = torch.zeros((pps, P), dtype=torch.int32, device=dev)
+            d_proj = torch.zeros((pps, fs), dtype=torch.float64, device=dev)
 
-    points = args.steps * pps * pts_per_pair * world
-    total_s, kern_ms, clocks = timed(args.form)
-    value = points / total_s
-    plain = None
-    if args.form != "fp64" and not args.no_compare:
-        p_s, p_kern_ms, p_clocks = timed("fp64")
-        plain = {"value": points / p_s, "ms_per_step": 1e3 * p_s / args.steps, "clocks": p_clocks}
-    else:
-        p_kern_ms = kern_ms
-    ctx.set_form(args.form)
+        def step(k, ev=None):
+            off = d_uv.data_ptr() + k * pps * per_pair_uv
+            if ev:
+                ev[0].record(stream)
+            ctx.batch_device(pps, off, d_z.data_ptr(), d_st.data_ptr(), sh)
+            ctx.project_device(pps, d_z.data_ptr(), d_proj.data_ptr(), True, sh)
+            if ev:
+                ev[1].record(stream)
+
+        out = {}
+        for form in forms:
+            ctx.set_form(form)
+            ctx.set_timing(False)
+            with torch.cuda.stream(stream):
+                for k in range(warmup):
+                    flush.zero_()
+                    step(k)
+                torch.cuda.synchronize()
+                if dist:
+                    dist.barrier()
+                evs = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(steps)]
+                ctx.set_timing(True)
+                with ClockSampler(clock_path(args, f"{tag}_{form}_rank{rank}")) as clk:
+                    torch.cuda.synchronize()
+                    for k in range(steps):
+                        flush.zero_()
+                        step(warmup + k, evs[k])
+                    torch.cuda.synchronize()
+                if dist:
+                    dist.barrier()
+            stages = ctx.stage_times()
+            ctx.set_timing(False)
+            tot = sum(e[0].elapsed_time(e[1]) for e in evs) / 1e3
+            if dist:
+                t = torch.tensor([tot], device=dev)
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                tot = float(t)
+            status = d_st.cpu().numpy()
+            if (status & ~1).any():
+                raise RuntimeError(f"non-trivial point status flags ({tag}, {form}): {np.unique(status)}")
+            out[form] = {"total_s": tot, "ms_per_step": 1e3 * tot / steps,
+                         "stage_ms_per_step": {k: v / steps for k, v in stages.items()},
+                         "clocks": clk.summary(local_rank)}
+        return out, packed
+
+    # ---- the headline workload in every form
+    forms = [args.form] + [f for f in (args.compare_forms.split(",") if args.compare_forms else FORMS)
+                           if f and f != args.form]
+    ctx = PnampContext(wl.sp, wl.e0, wl.t1b, wl.recs, wl.vbar, wl.mesh, q2=wl.q2)
+    P, G = ctx.n_euler, wl.mesh.n_gauge
+    res, packed = timed_forms(wl, ctx, order, forms, args.steps, args.warmup, "pf")
+    pts_step = pps * P * G
+    points = args.steps * pts_step * world
+    head = res[args.form]
+    value = points / head["total_s"]
 
     # ---- e2e through the host-buffer C ABI, pinned host memory
     e2e = None
     if not args.no_e2e:
+        ctx.set_form(args.form)
         pin = torch.empty(packed.shape, dtype=torch.float64).pin_memory().numpy()
         pin[...] = packed
-        h2d = pps * per_pair_uv + pps * 19 * P * 16
+        per_pair_uv = packed[0].nbytes
+        h2d = pps * per_pair_uv
         d2h = pps * 19 * P * 16 + pps * P * 4 + pps * fs * 8
         for k in range(min(args.warmup, 1)):
             ctx.batch(pin[k * pps:(k + 1) * pps])
@@ -543,50 +605,110 @@ def main():
             te = float(t)
         e2e = {"value": points / te, "unit": "points/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
+    ctx.close()
 
-    # ---- rooflines of the dominant kernel (the point kernel; setup is < 0.1 %). The FP64
-    # form is bound by the FP64 pipe; the double-float form does the same algorithmic
-    # work on the FP32 pipes, so its FP64-equivalent rate may exceed the FP64 peak.
-    flops_pt = algorithmic_flops_per_point(wl, G)
-    pts_launch = pps * pts_per_pair
-    peak = fp64_peak_tflops(torch) if rank == 0 else None
-    ach_form = flops_pt * pts_launch / (statistics.mean(kern_ms) / 1e3) / 1e12
-    ach_plain = flops_pt * pts_launch / (statistics.mean(p_kern_ms) / 1e3) / 1e12
+    # ---- the general path: the same set with proton-neutron mixing vacua, and the reference's
+    # own Ti48 / KB3G vacua and interaction, on the same mesh
+    secondary = {}
+    if not args.no_general:
+        steps2 = max(1, min(args.steps, args.secondary_steps))
+        for tag, w2, forms2 in (("pf_pnmix", config(1, pn_mix=True), [f for f in FORMS]),
+                                ("ti48_kb3g", ti48_workload(wl.mesh), ["df64", args.form]
+                                 if args.form != "df64" else ["df64", "fp64"])):
+            if args.mesh:
+                w2.mesh = wl.mesh
+            mine2 = rank_pairs(w2.pairs, rank, world)
+            order2 = [mine2[k % len(mine2)] for k in range((1 + steps2) * pps)]
+            c2 = PnampContext(w2.sp, w2.e0, w2.t1b, w2.recs, w2.vbar, w2.mesh, q2=w2.q2)
+            r2, _ = timed_forms(w2, c2, order2, list(dict.fromkeys(forms2)), steps2, 1, tag)
+            c2.close()
+            pts2 = steps2 * pps * w2.mesh.n_euler * w2.mesh.n_gauge * world
+            paths = _pair_paths(w2, order2[pps:])
+            secondary[tag] = {
+                "workload": ("pf shell n=40, 20 seeded deformed vacua mixing protons and neutrons, same mesh "
+                             "(general path)" if tag == "pf_pnmix" else
+                             "Ti48 / KB3G (pf shell, Z=2, N=6 valence), the reference's 8 HFB vacua with "
+                             "proton-neutron pairing and its m-scheme interaction file, same mesh (general path)"),
+                "pairs_timed": len(order2) - pps, "species_split_pairs": sum(a for a, _ in paths),
+                "reduced_pfaffian_pairs": sum(b for _, b in paths),
+                "forms": {f: {"value": pts2 / v["total_s"], "ms_per_step": v["ms_per_step"],
+                              "stage_ms_per_step": v["stage_ms_per_step"]} for f, v in r2.items()}}
+
+    # ---- rooflines from the library's per-launch events over the timed steps
+    timed_pairs = order[args.warmup * pps:]
+    peaks = measured_peaks()
+    tf64 = gemm_peak_tflops(torch, torch.float64) if rank == 0 else None
+    tf32 = gemm_peak_tflops(torch, torch.float32, 8192) if rank == 0 else None
+    rl = {}
+    for form, v in res.items():
+        tc = form.startswith("tc")
+        flops_pt = algorithmic_flops_per_point(wl, G, timed_pairs, records=not tc)
+        t_pts = v["stage_ms_per_step"]["points"] / 1e3
+        ach = flops_pt * pts_step / t_pts / 1e12
+        if form == "fp64":
+            rl[form] = {"kernel": "point_kernel<FP64>", "bound": "fp64", "flops_per_point": flops_pt,
+                        "achieved": ach, "peak": tf64, "unit": "TFLOP/s", "frac": ach / tf64 if tf64 else None,
+                        "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                        "traffic": TRAFFIC_BYTES_PER_POINT["fp64"] * pts_step}
+        else:
+            fp32 = 2.0 * FP32_INSTR_PER_FLOP * ach   # FP32 flop rate of the double-float instructions
+            rl[form] = {"kernel": "point_kernel<double-float>", "bound": "fp32", "flops_per_point": flops_pt,
+                        "fp64_equivalent_tflops": ach, "achieved": fp32, "peak": tf32, "unit": "TFLOP/s",
+                        "frac": fp32 / tf32 if tf32 else None,
+                        "peak_source": "cuBLAS SGEMM 8192^3 measured in this run; achieved = FP64-equivalent "
+                                       f"flops x {FP32_INSTR_PER_FLOP} FP32 instructions x 2 (FMA)",
+                        "traffic": TRAFFIC_BYTES_PER_POINT["df64"] * pts_step}
+        if tc:
+            gf = gemm_flops_per_point(wl.sp)
+            t_c = v["stage_ms_per_step"]["contract"] / 1e3
+            bf = peaks.get("bf16_tflops_sustained")
+            achc = gf * pts_step / t_c / 1e12 if t_c > 0 else None
+            nprod = 3 if form == "tc3" else 6
+            rl[form]["contraction"] = {
+                "kernel": f"contract_kernel<{2 if form == 'tc3' else 3}> (tcgen05 kind::f16, TMA, TMEM)",
+                "bound": "tensor", "flops_per_point": gf, "achieved": achc, "peak": bf, "unit": "TFLOP/s",
+                "frac": achc / bf if achc and bf else None,
+                "executed_tflops": achc * nprod if achc else None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (a kernel inside a long step)",
+                "note": f"algorithmic = one product of the dense group GEMMs; {form} executes {nprod}"}
 
     cpu = None
-    if pool is not None:
-        _, dt = cpu_sample(pool, ncores, wl, ncores)
-        nsamp = max(ncores, int(ncores * max(1.0, args.cpu_seconds / max(dt, 1e-3))))
-        rate, dt = cpu_sample(pool, ncores, wl, nsamp)
-        pool.close()
-        cpu = {"value": rate, "unit": "points/s", "cores": ncores, "kind": "port",
-               "sample": f"{nsamp} Euler points x 81 gauge points of pair (0,0), {dt:.1f} s, "
-                         f"oracle/pnamp_oracle.py on a spawn pool of {ncores} processes"}
+    if not args.no_cpu_baseline and rank == 0 and world == 1:
+        from oracle import cpu_baseline as cb
+        cb.build()
+        nth = cb.max_threads()
+        sample_pairs = order[args.warmup * pps:args.warmup * pps + pps]
+        r_all, t_all, p_all = cpu_calibrated(wl, sample_pairs, args.cpu_seconds)
+        r_one, t_one, p_one = cpu_calibrated(wl, sample_pairs, args.cpu_seconds / 3, threads=1)
+        r_imp, t_imp, p_imp = cpu_calibrated(wl, sample_pairs, args.cpu_seconds / 3, form="as_implemented")
+        cpu = {"value": r_all, "unit": "points/s", "cores": nth, "kind": "port",
+               "sample": f"{p_all} points (Euler points x all gauge points) of the first timed step's {pps} pairs, "
+                         f"{t_all:.1f} s; oracle/cpu/pnamp_cpu.cpp minimal form on {nth} OpenMP threads",
+               "one_core": {"value": r_one, "points": p_one, "seconds": t_one},
+               "as_implemented": {"value": r_imp, "cores": nth, "points": p_imp, "seconds": t_imp,
+                                  "note": "the reference's per-point ZGEMM / LU / 2n x 2n Pfaffian sequence"}}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * total_s / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "df64" if args.form == "df64" else "f64",
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp64": "f64", "df64": "df64", "tc3": "df64+bf16x3", "tc6": "df64+bf16x6"}[args.form],
             "data": "synthetic: seeded vacua and TBMEs (no public dataset exists)",
-            "config": {"workload": WORKLOAD, "form": FORM_TEXT[args.form], "pairs_per_step": pps,
-                       "points_per_pair": pts_per_pair, "l2": "flushed (256 MiB write) before each step",
-                       "parallelism": f"pairs round-robin over {world} rank(s)"},
-            "roofline": {"bound": "fp64", "achieved": ach_plain, "peak": peak, "unit": "TFLOP/s",
-                         "frac": (ach_plain / peak) if peak else None,
-                         "traffic": TRAFFIC_BYTES_PER_POINT * pts_launch,
-                         "kernel": "point_kernel<FP64>", "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
-                         "flops_per_point": flops_pt,
-                         "df64_fp64_equivalent": {"achieved": ach_form, "frac_of_fp64_peak":
-                                                  (ach_form / peak) if peak else None}},
-            "plain_fp64": plain,
+            "config": line_config,
+            "roofline": dict(rl[args.form]),
+            "forms": {f: {"value": points / v["total_s"], "ms_per_step": v["ms_per_step"],
+                          "stage_ms_per_step": v["stage_ms_per_step"], "text": FORM_TEXT[f],
+                          "roofline": rl[f], "clocks": v["clocks"]} for f, v in res.items()},
+            "plain_fp64": ({"value": points / res["fp64"]["total_s"], "ms_per_step": res["fp64"]["ms_per_step"]}
+                           if "fp64" in res else None),
+            "general_path": secondary or None,
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "clocks": clocks,
-            "gpu_launches": 3 * args.steps,
+            "clocks": head["clocks"],
+            "gpu_launches": args.steps * (4 if args.form.startswith("tc") else 3),
         }
         print(json.dumps(line))
-    ctx.close()
     if dist:
         dist.destroy_process_group()
     return 0

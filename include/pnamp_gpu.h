@@ -300,9 +300,10 @@ int pnamp_sync(pnamp_ctx *ctx);
 /* Stage timing (no counterpart in the reference, whose timers are commented out,
  * PNAMP_Kernel3D.f90:189-192,241-242): with `on` set, each later pnamp_batch_device /
  * pnamp_batch_items_device call records CUDA events around its launches on the launching
- * stream; pnamp_stage_times waits for the last call's events and writes the summed
- * milliseconds of its stages to ms[4] = {setup, point kernel, tensor-core contraction,
- * contraction sum into ZRES}, returning 4 (or an error code). */
+ * stream (no host synchronisation); pnamp_stage_times waits for those events and writes the
+ * milliseconds of the calls since pnamp_set_timing or the previous pnamp_stage_times, summed
+ * per stage, to ms[4] = {setup, point kernel, tensor-core contraction, contraction sum into
+ * ZRES}, returning 4 (or an error code). */
 int pnamp_set_timing(pnamp_ctx *ctx, int on);
 int pnamp_stage_times(pnamp_ctx *ctx, double *ms);
 

@@ -1011,7 +1011,6 @@ int pnamp_batch_device(pnamp_ctx *c, int npairs, const double *d_uv, double *d_z
     int rc = ensure_pairs(c, npairs);
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
-    c->ev_marks.clear();
     if (c->tc_splits) return tc_run(c, npairs, d_uv, d_zres, d_status, st, nullptr, 0);
     int mk = stage_begin(c, st);
     CK(launch_setup(c->p, npairs, d_uv, c->d_pairbuf, st));
@@ -1030,7 +1029,6 @@ int pnamp_batch_items_device(pnamp_ctx *c, int npairs, const double *d_uv, long 
     int rc = ensure_pairs(c, npairs);
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;  // NULL: legacy default stream
-    c->ev_marks.clear();
     if (c->tc_splits) {
         if (d_gauge_out) return PNAMP_ERR_STATE;  // per-gauge H/N would lack the contracted energy
         return tc_run(c, npairs, d_uv, d_zres, d_status, st, d_items, nitems);
@@ -1448,6 +1446,7 @@ int pnamp_stage_times(pnamp_ctx *c, double *ms) {
         CK(cudaEventElapsedTime(&t, c->ev_pool[m[1]], c->ev_pool[m[2]]));
         ms[m[0]] += t;
     }
+    c->ev_marks.clear();
     return kStages;
 }
 

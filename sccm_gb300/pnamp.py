@@ -485,11 +485,10 @@ class PnampContext:
             raise PnampError(rc, "pnamp_set_timing")
 
     def stage_times(self):
-        """ms of the last batch call's stages: dict(setup, points, contract, finish)."""
+        """ms per stage of the batch calls since set_timing or the previous stage_times, summed:
+        dict(setup, points, contract, finish)."""
         ms = np.zeros(4)
         rc = load_library().pnamp_stage_times(self._h, ms.ctypes.data)
-        if rc < 0 or rc > 4 and rc != 4:
-            raise PnampError(rc, "pnamp_stage_times")
         if rc != 4:
             raise PnampError(rc, "pnamp_stage_times")
         return dict(zip(("setup", "points", "contract", "finish"), ms.tolist()))

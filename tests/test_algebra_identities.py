@@ -19,6 +19,7 @@ import pytest
 
 from sccm_gb300.basis import SHELLS, ModelSpace
 from sccm_gb300.synth import mscheme_pairs
+from sccm_gb300.contraction import contraction_groups
 from oracle.pnamp_oracle import Hamiltonian, energy, zpfaffian
 
 rng = np.random.default_rng(20261203)
@@ -113,73 +114,6 @@ def test_column_gauss_jordan_with_row_pivoting():
                     if j != k:
                         row[j] -= m * P[j]
         assert np.abs(W - Y @ np.linalg.inv(A)).max() <= 1e-10 * np.abs(Y @ np.linalg.inv(A)).max()
-
-
-def contraction_groups(sp, recs, vbar, cap=256):
-    """Restatement of pnamp_capi.cu::build_tc: storage position and group of every ph entry
-    (r, c) and pp pair (i < j), and each group's dense square matrix."""
-    n = sp.nlev
-    m, t, l = sp.twom.astype(int), sp.t.astype(int), sp.l.astype(int)
-    ph, pp = {}, {}
-    for r in range(n):
-        for c in range(n):
-            ph.setdefault((m[r] - m[c], t[r] - t[c], (l[r] + l[c]) % 2), []).append((r, c))
-    for i in range(n):
-        for j in range(i + 1, n):
-            pp.setdefault((m[i] + m[j], t[i] + t[j], (l[i] + l[j]) % 2), []).append((i, j))
-    ph_units = []
-    for L in sorted(ph):
-        N = (-L[0], -L[1], L[2])
-        if N < L and N in ph:
-            continue
-        ph_units.append([L] if N == L or N not in ph else [L, N])
-    pp_units = [[L] for L in sorted(pp)]
-
-    def pack(units, mem):
-        order = sorted(range(len(units)), key=lambda u: -sum(len(mem[k]) for k in units[u]))
-        groups, fill = [], []
-        for u in order:
-            sz = sum(len(mem[k]) for k in units[u])
-            for g in range(len(groups)):
-                if fill[g] + sz <= cap:
-                    groups[g] += units[u]
-                    fill[g] += sz
-                    break
-            else:
-                groups.append(list(units[u]))
-                fill.append(sz)
-        return groups
-    pos, grp, ranges = {}, {}, []
-    off = 0
-    for kind, groups, mem in (("ph", pack(ph_units, ph), ph), ("pp", pack(pp_units, pp), pp)):
-        for g in groups:
-            d = 0
-            for L in g:
-                for e in mem[L]:
-                    pos[(kind, e)] = off + d
-                    grp[(kind, e)] = len(ranges)
-                    d += 1
-            dpad = -(-d // 64) * 64
-            ranges.append((kind, off, dpad))
-            off += dpad
-    mats = [np.zeros((dp, dp)) for _, _, dp in ranges]
-
-    def add(kind, e1, e2, v):
-        g = grp[(kind, e1)]
-        assert grp[(kind, e2)] == g
-        o = ranges[g][1]
-        mats[g][pos[(kind, e1)] - o, pos[(kind, e2)] - o] += v
-    for (i, j, k, ll), V in zip(recs, vbar):
-        d = 0.0 if i + j == k + ll else 1.0
-        add("ph", (k, i), (ll, j), V)
-        add("ph", (ll, i), (k, j), -V)
-        if d:
-            add("ph", (i, k), (j, ll), V)
-            add("ph", (j, k), (i, ll), -V)
-        add("pp", (i, j), (k, ll), V / 4)
-        if d:
-            add("pp", (k, ll), (i, j), V / 4)
-    return pos, ranges, mats, off
 
 
 @pytest.mark.parametrize("shell", ["sd", "pf", "sdpf"])
