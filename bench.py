@@ -416,7 +416,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target length of the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--form", default="df64", choices=list(FORMS),
+    ap.add_argument("--form", default="tc6", choices=list(FORMS),
                     help="headline arithmetic form: plain FP64, double-float, or double-float with the "
                          "two-body contraction on the tensor cores (BF16x3, BF16x6)")
     ap.add_argument("--compare-forms", default=None,
@@ -424,6 +424,8 @@ def main():
     ap.add_argument("--no-general", action="store_true",
                     help="skip the general-path workloads (pn-mixing vacua, Ti48/KB3G)")
     ap.add_argument("--secondary-steps", type=int, default=3, help="timed steps of the general-path workloads")
+    ap.add_argument("--pn-mix", action="store_true",
+                    help="headline workload with proton-neutron mixing vacua (the general path), e.g. for profiles")
     ap.add_argument("--mesh", default=None,
                     help="override the mesh as NALP,NBET,NGAM,NFOM (small cases for profiling captures)")
     ap.add_argument("--workload", default="pf", choices=["pf", "uneven", "learned", "rho2b"],
@@ -454,13 +456,18 @@ def main():
     from sccm_gb300.basis import Mesh
     from sccm_gb300.driver import rank_pairs
     from sccm_gb300.synth import config, ti48_workload
-    wl = config(1)
+    wl = config(1, pn_mix=args.pn_mix)
     if args.mesh:
         wl.mesh = Mesh(*[int(x) for x in args.mesh.split(",")])
     pps = args.pairs_per_step
     mine = rank_pairs(wl.pairs, rank, world)
     order = [mine[k % len(mine)] for k in range((args.warmup + args.steps) * pps)]
-    line_config = {"workload": WORKLOAD, "form": FORM_TEXT[args.form], "pairs_per_step": pps,
+    workload = WORKLOAD if not args.pn_mix else WORKLOAD.replace(
+        "seeded deformed charge-conserving vacua", "seeded deformed vacua mixing protons and neutrons").replace(
+        "(species-split path)", "(general path)")
+    if args.mesh:
+        workload += f", mesh overridden to {args.mesh}"
+    line_config = {"workload": workload, "form": FORM_TEXT[args.form], "pairs_per_step": pps,
                    "points_per_pair": wl.mesh.n_euler * wl.mesh.n_gauge,
                    "l2": "flushed (256 MiB write) before each step",
                    "parallelism": f"pairs round-robin over {world} rank(s)"}

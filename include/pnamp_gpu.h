@@ -263,7 +263,9 @@ int pnamp_project_rho2b(pnamp_ctx *ctx, const double *zres, const double *rho2b,
  * one CTA workspace exceed the array is rejected with PNAMP_ERR_SCRATCH_LIMIT;
  * otherwise the grid shrinks to the CTA workspaces that fit. The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress) and caches
- * it; make that first call before any stream capture. All calls share the array
+ * it; make that first call before any stream capture. The cached address
+ * assumes the device's context lives for the rest of the process (no
+ * cudaDeviceReset after the first call). All calls share the array
  * and it keeps the last call's contents; the kernels write every scratch byte
  * before reading it, so nothing is cleared. Calls whose work overlaps on the GPU
  * (different streams, or different host threads) race on the array: serialise

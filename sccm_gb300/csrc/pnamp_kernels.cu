@@ -287,14 +287,15 @@ __device__ bool gj_right_solve(T *A, int n, T *Y, int ny, T *prow, T *pinv, int 
     return sing;
 }
 
-// gj_right_solve for two independent systems at once, by the thread group g (at least
-// 2 warps plus h threads; warps 0 and 1 of the group search the pivots): A holds two h x h matrices
-// (compact, the second at A + h*h) and Y two ny x h blocks (the second at Y + ny*h);
-// Y_b <- Y_b A_b^-1 for b = 0, 1 in h steps of two barriers (warp b searches the pivots
-// of system b). prow holds 2h scratch values, pinv 2, sh 4 ints. Returns true if an
-// exactly zero pivot row was met in either system.
-template <typename T>
-__device__ bool gj_right_solve2(const Grp &g, T *A, int h, T *Y, int ny, T *prow, T *pinv, int *sh) {
+// gj_right_solve for NB = 1 or 2 independent systems at once, by the thread group g (at
+// least NB warps plus h threads; warp b of the group searches the pivots of system b): A holds
+// NB h x h matrices (compact, the second at A + h*h) and Y NB ny x h blocks (the second at
+// Y + ny*h); Y_b <- Y_b A_b^-1 in h steps of two group barriers. prow holds NB*h scratch
+// values, pinv NB, sh 2*NB ints. Returns true if an exactly zero pivot row was met in any
+// system. NB = 2 serves the two species blocks of a species-split point, NB = 1 the whole
+// n x n system of a general point while other warps eliminate its Pfaffian.
+template <typename T, int NB = 2>
+__device__ bool gj_right_solve_g(const Grp &g, T *A, int h, T *Y, int ny, T *prow, T *pinv, int *sh) {
     const int lane = g.tid & 31, wid = g.wid;
     const int hh = h * h, yh = ny * h;
     auto search = [&](int b, int k) {  // warp b: pivot column of row k of A_b
@@ -326,18 +327,19 @@ __device__ bool gj_right_solve2(const Grp &g, T *A, int h, T *Y, int ny, T *prow
         }
     };
     bool sing = false;
-    // phase-2 layout of warps 2..: rpi rows at a time, one column per thread
-    const int rpi = (g.nthr - 64) / h, jc = (g.tid - 64) % h, r0 = (g.tid - 64) / h;
-    if (wid < 2) search(wid, 0);
+    // phase-2 layout of warps NB..: rpi rows at a time, one column per thread
+    constexpr int kRes = 32 * NB;
+    const int rpi = (g.nthr - kRes) / h, jc = (g.tid - kRes) % h, r0 = (g.tid - kRes) / h;
+    if (wid < NB) search(wid, 0);
     gsync(g);
     for (int k = 0; k < h; ++k) {
-        const int c0 = sh[0], c1 = sh[2];
-        if (sh[1] || sh[3]) sing = true;
-        const T pv0 = pinv[0], pv1 = pinv[1];
-        // phase 1 (both systems): m_r = M[r][c] / A[k][c] into column k, old column k into
+        const int c0 = sh[0], c1 = NB > 1 ? sh[2] : 0;
+        if (sh[1] || (NB > 1 && sh[3])) sing = true;
+        const T pv0 = pinv[0], pv1 = NB > 1 ? pinv[1] : pinv[0];
+        // phase 1 (all systems): m_r = M[r][c] / A[k][c] into column k, old column k into
         // column c, the exchanged pivot row into prow
         const int nrT = h - k - 1, nrows = nrT + ny, per1 = nrows + h;
-        for (int t = g.tid; t < 2 * per1; t += g.nthr) {
+        for (int t = g.tid; t < NB * per1; t += g.nthr) {
             const int b = t >= per1 ? 1 : 0, u = t - b * per1;
             const int c = b ? c1 : c0;
             T *Ab = A + b * hh;
@@ -353,7 +355,7 @@ __device__ bool gj_right_solve2(const Grp &g, T *A, int h, T *Y, int ny, T *prow
         }
         gsync(g);
         // phase 2: M[r][j] -= m_r prow[j] for j != k; warp b takes row k + 1 of A_b, then its pivot
-        if (wid < 2) {
+        if (wid < NB) {
             if (k + 1 < h) {
                 T *row = A + wid * hh + (k + 1) * h;
                 const T m = row[k];
@@ -363,12 +365,12 @@ __device__ bool gj_right_solve2(const Grp &g, T *A, int h, T *Y, int ny, T *prow
                 search(wid, k + 1);
             }
         } else if (r0 < rpi && jc != k) {
-            // thread (r0, jc): column jc of every rpi-th row of both systems; the pivot-row
+            // thread (r0, jc): column jc of every rpi-th row of all systems; the pivot-row
             // values stay in registers and m_r = row[k] is a broadcast load
             const int nrA = h - k - 2 > 0 ? h - k - 2 : 0;
             const int rows_b = nrA + ny;
-            const T pj0 = prow[jc], pj1 = prow[h + jc];
-            for (int R = r0; R < 2 * rows_b; R += rpi) {
+            const T pj0 = prow[jc], pj1 = NB > 1 ? prow[h + jc] : pj0;
+            for (int R = r0; R < NB * rows_b; R += rpi) {
                 const int b = R >= rows_b ? 1 : 0, rr = R - b * rows_b;
                 T *row = rr < nrA ? A + b * hh + (k + 2 + rr) * h : Y + b * yh + (rr - nrA) * h;
                 row[jc] = sfms(row[k], b ? pj1 : pj0, row[jc]);
@@ -551,8 +553,10 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &u
 // elimination runs on (its values are discarded): the result is 0 with `underflow` set.
 // Returns Pf(first) * Pf(second) and `underflow` in the group's thread 0. `vec` holds 2h
 // scratch values, `pv` 4 (pivots and reciprocals), `flag` 4 ints.
-template <class Z>
-__device__ zc pfaffian_upper2(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *flag, int &underflow) {
+// NB = 1 is the same elimination of one h x h matrix (a general point's n x n Schur
+// complement, eliminated while the other warps run the Gauss-Jordan solve).
+template <class Z, int NB = 2>
+__device__ zc pfaffian_upper_g(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *flag, int &underflow) {
     using A = Ar<Z>;
     const int lane = g.tid & 31, wid = g.wid;
     const int hh = h * h;
@@ -592,21 +596,21 @@ __device__ zc pfaffian_upper2(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fla
             pv[2 + b] = f ? ssz : zrecip(ssz);
         }
     };
-    if (nstep > 0 && wid < 2) search(wid, 0);
+    if (nstep > 0 && wid < NB) search(wid, 0);
     gsync(g);
     for (int k = 0; k < nstep; ++k) {
         const int r = 2 * k, c = r + 1;
-        const int q0 = flag[0], q1 = flag[1];
+        const int q0 = flag[0], q1 = NB > 1 ? flag[1] : 0;
         if (g.tid == 0) {
-            const int fk = flag[2] > flag[3] ? flag[2] : flag[3];
+            const int fk = (NB > 1 && flag[3] > flag[2]) ? flag[3] : flag[2];
             if (uf == 0) uf = fk;  // the first failing step decides, as the early return did
-            for (int b = 0; b < 2; ++b) {
+            for (int b = 0; b < NB; ++b) {
                 const double phas = ((b ? q1 : q0) == c) ? 1.0 : -1.0;
                 pf = phas * (pf * A::to(pv[b]));
             }
         }
-        // (a) exchange c <-> q (exch_upper on both matrices) and v_i = S'[c][i] / S'[r][c], i > c
-        for (int t = g.tid; t < 2 * (h - r); t += g.nthr) {
+        // (a) exchange c <-> q (exch_upper on every matrix) and v_i = S'[c][i] / S'[r][c], i > c
+        for (int t = g.tid; t < NB * (h - r); t += g.nthr) {
             const int b = t / (h - r), i = r + t % (h - r);
             const int q = b ? q1 : q0;
             const Z inv = pv[2 + b];
@@ -641,7 +645,7 @@ __device__ zc pfaffian_upper2(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fla
         gsync(g);
         // (b) S_ij += v_i S_rj - S_ri v_j for c < i < j; row c + 1 (the next pivot row) first
         const bool more = k + 1 < nstep;
-        if (wid < 2) {
+        if (wid < NB) {
             Z *Sb = S + wid * hh;
             const Z *vb = vec + wid * h;
             const int i = c + 1;
@@ -656,7 +660,7 @@ __device__ zc pfaffian_upper2(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fla
             if (more) search(wid, c + 1);
         }
         const int mm = h - c - 2, TT = mm * (mm - 1) / 2;
-        for (int t = g.tid; t < 2 * TT; t += g.nthr) {
+        for (int t = g.tid; t < NB * TT; t += g.nthr) {
             const int b = t / TT;
             int i, j;
             tri_index(t - b * TT, mm, i, j);
@@ -672,7 +676,8 @@ __device__ zc pfaffian_upper2(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fla
         gsync(g);
     }
     if (g.tid == 0) {
-        pf = pf * A::to(S[(h - 2) * h + h - 1]) * A::to(S[hh + (h - 2) * h + h - 1]);
+        pf = pf * A::to(S[(h - 2) * h + h - 1]);
+        if (NB > 1) pf = pf * A::to(S[hh + (h - 2) * h + h - 1]);
         if (uf) pf = mk(0.0, 0.0);
     }
     underflow = uf;
@@ -1004,9 +1009,44 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 // two-barrier Pfaffian 2, 3 and 4 Pfaffian warps time within 0.4 % of each other,
                 // so the solve keeps 14). One CTA barrier joins them before the densities.
                 const bool conc = split && !onishi;
+                // general reduced points (vacua that mix protons and neutrons): the same overlap of
+                // the n x n Schur complement's elimination (warps 0 .. kPfWarpsG-1, named barrier 1)
+                // with the n x n Gauss-Jordan solve on the other warps (named barrier 2)
+                const bool concg = !split && reduced && !onishi;
                 int under = 0;
                 zc pf = mk(0.0, 0.0);
                 bool sing = false;
+                if (concg) {
+                    constexpr int kPfWarpsG = 4;
+                    if (wid < kPfWarpsG) {
+                        const Grp g{(int)threadIdx.x, kPfWarpsG * 32, wid, 1};
+                        for (int t = g.tid; t < n * (n - 1) / 2; t += g.nthr) {
+                            int i, j;
+                            tri_index(t, n, i, j);
+                            const Z dd_ = (j < h) ? dpp : ((i < h) ? dpn : dnn);
+                            S[i * n + j] = X[i * n + j] * dd_ + A::from(mk(-p.cscale * gZi[i * n + j], 0.0));
+                        }
+                        gsync(g);
+                        pf = pfaffian_upper_g<Z, 1>(g, S, n, vec, reinterpret_cast<Z *>(red + kPfScratch), sh, under);
+                        pf = pf * pfz;  // meaningful in thread 0
+                    } else if (!p.norm_only) {
+                        const Grp g{(int)threadIdx.x - kPfWarpsG * 32, (int)blockDim.x - kPfWarpsG * 32,
+                                    wid - kPfWarpsG, 2};
+                        for (int t = g.tid; t < nn; t += g.nthr) {
+                            Z sv = zep * P[t];
+                            sv = zfma(zen, P[nn + t], sv);
+                            sv = zfma(zepc, P[2 * nn + t], sv);
+                            sv = zfma(zenc, P[3 * nn + t], sv);
+                            T[t] = sv;
+                        }
+                        for (int t = g.tid; t < 2 * nn; t += g.nthr) Y[t] = B[t];
+                        gsync(g);
+                        const bool sg = gj_right_solve_g<Z, 1>(g, T, n, Y, 2 * n, invd, vec + n, sh + 4);
+                        if (g.tid == 0) sh[4] = sg ? 1 : 0;
+                    }
+                    __syncthreads();
+                    if (!p.norm_only) sing = sh[4] != 0;
+                }
                 if (conc) {
                     constexpr int kPfWarps = 2;  // the two pivot searches need one warp each
                     if (wid < kPfWarps) {
@@ -1022,7 +1062,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                             S[b * h * h + i * h + j] = v;
                         }
                         gsync(g);
-                        pf = pfaffian_upper2<Z>(g, S, h, vec, reinterpret_cast<Z *>(red + kPfScratch), sh, under);
+                        pf = pfaffian_upper_g<Z, 2>(g, S, h, vec, reinterpret_cast<Z *>(red + kPfScratch), sh, under);
                         pf = pf * pfz;  // meaningful in thread 0
                     } else if (!p.norm_only) {
                         const Grp g{(int)threadIdx.x - kPfWarps * 32, (int)blockDim.x - kPfWarps * 32,
@@ -1042,13 +1082,13 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                             Y[t] = B[grow * n + b * h + j];
                         }
                         gsync(g);
-                        const bool sg = gj_right_solve2<Z>(g, T, h, Y, 2 * h, invd, vec + 2 * h, sh + 4);
+                        const bool sg = gj_right_solve_g<Z, 2>(g, T, h, Y, 2 * h, invd, vec + 2 * h, sh + 4);
                         if (g.tid == 0) sh[4] = sg ? 1 : 0;
                     }
                     __syncthreads();
                     if (!p.norm_only) sing = sh[4] != 0;
                 }
-                for (int t = threadIdx.x; t < (onishi || split ? 0 : NP * (NP - 1) / 2); t += blockDim.x) {
+                for (int t = threadIdx.x; t < (onishi || split || concg ? 0 : NP * (NP - 1) / 2); t += blockDim.x) {
                     int i, j;
                     tri_index(t, NP, i, j);
                     Z v;
@@ -1063,8 +1103,8 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     }
                     S[i * NP + j] = v;
                 }
-                if (!conc) __syncthreads();
-                if (conc) {
+                if (!conc && !concg) __syncthreads();
+                if (conc || concg) {
                 } else if (onishi) {
                     // Onishi (PNAMP_Onishi.f90:21-37): sqrt(det(Ubar^T U0 + Vbar^T V0)),
                     // Ubar = R U1, Vbar = conj(R) V1 at phi = 0; LU determinant, principal root
@@ -1120,7 +1160,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     if (!conc) {  // (Onishi norm) the whole CTA solves after the norm
                         __syncthreads();
                         const Grp gall{(int)threadIdx.x, (int)blockDim.x, wid, 0};
-                        sing = gj_right_solve2<Z>(gall, T, h, Y, 2 * h, invd, vec, sh);
+                        sing = gj_right_solve_g<Z, 2>(gall, T, h, Y, 2 * h, invd, vec, sh);
                     }
                     // densities of each species block in one pass (rho, kappa10 and kappa01 of an
                     // entry share the loads of Y and V0^T), and zeros across the species
@@ -1149,16 +1189,18 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         S[q * n * ld + (b * h + i) * ld + (1 - b) * h + j] = zero;
                     }
                 } else {
-                for (int t = threadIdx.x; t < nn; t += blockDim.x) {
-                    Z s = zep * P[t];
-                    s = zfma(zen, P[nn + t], s);
-                    s = zfma(zepc, P[2 * nn + t], s);
-                    s = zfma(zenc, P[3 * nn + t], s);
-                    T[t] = s;
+                if (!concg) {  // (2n x 2n Pfaffian or Onishi norm) the whole CTA solves after the norm
+                    for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+                        Z s = zep * P[t];
+                        s = zfma(zen, P[nn + t], s);
+                        s = zfma(zepc, P[2 * nn + t], s);
+                        s = zfma(zenc, P[3 * nn + t], s);
+                        T[t] = s;
+                    }
+                    for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) Y[t] = B[t];
+                    __syncthreads();
+                    sing = gj_right_solve<Z>(T, n, Y, 2 * n, invd, vec, sh);
                 }
-                for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) Y[t] = B[t];
-                __syncthreads();
-                sing = gj_right_solve<Z>(T, n, Y, 2 * n, invd, vec, sh);
                 // ---- densities into the Pfaffian's storage, row stride ld
                 {
                     const int dq = blockDim.x / n, dr = blockDim.x % n;

@@ -133,3 +133,46 @@ def test_both_densities_in_one_pass(tmp_path):
     assert np.abs(r2 - r2s).max() <= 1e-13 * np.abs(r2s).max()   # atomic adds: order may differ
     assert len(read_rho1b_dens(tmp_path / rho1b_name(1, 2))) > 0
     assert len(read_rho2b_dat(tmp_path / rho2b_name(1, 2))) > 0
+
+
+@pytest.mark.parametrize("form", ["fp64", "df64"])
+def test_densities_device_entry_with_one_output(form):
+    """pnamp_batch_densities_device on the pf species-split path in both forms: with both
+    outputs it equals the single-density launches, with d_rho1b = NULL it writes only the
+    two-body sums and with d_rho2b = NULL only the one-body blocks; norm-only outputs are
+    refused."""
+    import ctypes as C
+    import torch
+    from sccm_gb300.pnamp import load_library
+    lib = load_library()
+    w = make_workload("pf", 2, Mesh(1, 2, 1, 3), seed=67)
+    pairs = [(*w.vacua[0], *w.vacua[1]), (*w.vacua[1], *w.vacua[1])]
+    dev = torch.device("cuda")
+    with ctx_for(w, form) as ctx:
+        _, _, r1s = ctx.batch_rho1b(pairs)
+        _, _, r2s = ctx.batch_rho2b(pairs)
+        nb, nq, P = r1s.shape[1], r2s.shape[1], ctx.n_euler
+        uv = torch.from_numpy(ctx.pack_pairs(pairs)).to(dev)
+        z = torch.zeros((2, 19 * P * 2), dtype=torch.float64, device=dev)
+        st = torch.zeros((2, P), dtype=torch.int32, device=dev)
+        out = {}
+        for which in ("both", "rho2b", "rho1b"):
+            r1 = torch.zeros((2, nb * P * 2), dtype=torch.float64, device=dev)
+            r2 = torch.zeros((2, nq * 2), dtype=torch.float64, device=dev)
+            p1 = None if which == "rho2b" else C.c_void_p(r1.data_ptr())
+            p2 = None if which == "rho1b" else C.c_void_p(r2.data_ptr())
+            rc = lib.pnamp_batch_densities_device(ctx.handle, 2, C.c_void_p(uv.data_ptr()), C.c_void_p(z.data_ptr()),
+                                                  C.c_void_p(st.data_ptr()), p1, p2, C.c_void_p(0))
+            torch.cuda.synchronize()
+            assert rc == 0, rc
+            out[which] = (r1.cpu().numpy().view(np.complex128).reshape(2, nb, P),
+                          r2.cpu().numpy().view(np.complex128).reshape(2, nq))
+        ctx.set_outputs("norm")
+        rc = lib.pnamp_batch_densities_device(ctx.handle, 2, C.c_void_p(uv.data_ptr()), C.c_void_p(z.data_ptr()),
+                                              C.c_void_p(st.data_ptr()), C.c_void_p(r1.data_ptr()), None,
+                                              C.c_void_p(0))
+        assert rc == PNAMP_ERR_STATE
+    scale2 = np.abs(r2s).max()
+    assert np.array_equal(out["both"][0], r1s) and np.abs(out["both"][1] - r2s).max() <= 1e-13 * scale2
+    assert np.abs(out["rho2b"][1] - r2s).max() <= 1e-13 * scale2 and not out["rho2b"][0].any()
+    assert np.array_equal(out["rho1b"][0], r1s) and not out["rho1b"][1].any()

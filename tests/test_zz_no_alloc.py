@@ -74,3 +74,36 @@ def test_noalloc_refuses_requests_beyond_its_scratch():
                                             C.c_void_p(0))
         torch.cuda.synchronize()
         assert rc == PNAMP_ERR_SCRATCH_LIMIT
+
+
+def test_noalloc_with_fewer_workspaces_than_ctas_allocates_nothing():
+    """120 pf pairs: their records fill a third of the array, so only ~110 CTA workspaces fit
+    (fewer than the 152-CTA grid of pnamp_batch_device) and the grid-stride loop runs on a cut
+    grid. Results equal pnamp_batch_device's, and the device's free memory does not move across
+    the call."""
+    lib = load_library()
+    w = make_workload("pf", 3, Mesh(1, 2, 1, 3), seed=406)
+    pairs = (w.pairs * 20)[:120]
+    with PnampContext(w.sp, w.e0, w.t1b, w.recs, w.vbar, w.mesh, q2=w.q2) as ctx:
+        n = w.sp.nlev
+        rec = (7 * n * n + 8) * 8
+        assert len(pairs) * rec > SCRATCH_BYTES // 4
+        packed = ctx.pack_pairs([(*w.vacua[i], *w.vacua[j]) for i, j in pairs])
+        z_ref, s_ref = _run(lib.pnamp_batch_device, ctx, packed)
+        _run(lib.pnamp_batch_device_noalloc, ctx, packed)          # first call: address lookup
+        dev = torch.device("cuda")
+        uv = torch.from_numpy(np.ascontiguousarray(packed)).to(dev)
+        z = torch.zeros((len(pairs), 19 * ctx.n_euler * 2), dtype=torch.float64, device=dev)
+        st = torch.zeros((len(pairs), ctx.n_euler), dtype=torch.int32, device=dev)
+        torch.cuda.synchronize()
+        free0, _ = torch.cuda.mem_get_info()
+        rc = lib.pnamp_batch_device_noalloc(ctx.handle, len(pairs), C.c_void_p(uv.data_ptr()),
+                                            C.c_void_p(z.data_ptr()), C.c_void_p(st.data_ptr()), C.c_void_p(0))
+        torch.cuda.synchronize()
+        free1, _ = torch.cuda.mem_get_info()
+        assert rc == 0 and free1 == free0
+        z_new = z.cpu().numpy().view(np.complex128).reshape(len(pairs), 19, ctx.n_euler)
+        assert np.array_equal(s_ref, st.cpu().numpy())
+        for k in range(len(pairs)):
+            scale = np.abs(z_ref[k, 0]).max()
+            assert np.abs(z_new[k, 0] - z_ref[k, 0]).max() <= NORM_TOL * scale
