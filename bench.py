@@ -62,7 +62,15 @@ FP32_INSTR_PER_FLOP = 7.5
 # DRAM bytes per kernel point of the point kernels (ncu dram__bytes_read + write on launches of
 # this workload, scaled by points): all per-point matrices live in shared memory or an
 # L2-resident slot, so traffic is tiny.
-TRAFFIC_BYTES_PER_POINT = {"fp64": (553984.0 + 2560.0) / 20736.0, "df64": 43.0}
+# DRAM bytes per point (dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture, divided
+# by the points of the launch): FP64 point kernel (20,736-point case), double-float point
+# kernel (20,736-point case: cold reads of the pair records and tables only), the
+# tensor-core forms' point kernel (5,184-point case: the bf16 density rows it writes,
+# 32 KB per point, which scale with the points) and the contraction kernel (5,184-point
+# case: those rows read back, plus the L2-resident group matrices)
+TRAFFIC_BYTES_PER_POINT = {"fp64": (553984.0 + 2560.0) / 20736.0, "df64": 43.0,
+                           "tc_point": (0.664064e6 + 166.103552e6) / 5184.0,
+                           "tc_contract": (212.85504e6 + 3.983616e6) / 5184.0}
 
 
 def _pair_paths(wl, pairs):
@@ -243,13 +251,15 @@ UNEVEN_WORKLOAD = ("uneven batch: 64 sd pairs (n=24, Euler 8x16x8, gauge 7x7), 1
 def learned_main(args):
     """`--workload learned`: learned + mixed against the exact mixed form on a fine-mesh pf set.
 
-    pf shell, `--learned-vacua` seeded deformed vacua (all symmetric pairs),
-    fine mesh 16 x 32 x 16 Euler x 11 x 11 gauge (991,232 points per pair),
-    coarse 4 x 8 x 4; the network (4 x 256) is trained on the first
-    `--learned-train` pairs. Reports both throughputs in fine-mesh points/s,
-    the fraction of Euler points computed exactly, and the errors of the
-    learned kernels against the exact ones (energy kernel in the basis of
-    normalised states, per-vacuum E_J, GCM levels).
+    The learned configuration: pf shell, `--learned-vacua` (40) seeded deformed vacua and
+    all their symmetric pairs (820), fine mesh 16 x 32 x 16 Euler x 11 x 11 gauge (991,232
+    points per pair), coarse 4 x 8 x 4; the network (4 x 256) is trained on
+    `--learned-train` (200) pairs spread over the set. The learned run ends with the
+    Hill-Wheeler gate (`LearnedPNAMP.run_gcm`). Reports both throughputs in fine-mesh
+    points/s, the fraction of Euler points computed exactly, the gate's record, and the
+    errors of the learned kernels against the exact ones (energy kernel in the basis of
+    normalised states, per-vacuum E_J, lowest GCM levels) with the 1 keV gates' verdict.
+    `--learned-ablation` adds the same method without the network.
     """
     import torch
     from sccm_gb300.basis import Mesh
@@ -258,8 +268,11 @@ def learned_main(args):
 
     torch.cuda.set_device(0)
     wl = make_workload("pf", args.learned_vacua, Mesh(16, 32, 16, 11), seed=4000)
-    lm = LearnedPNAMP(wl, LearnedConfig(train_euler=256, epochs=30, seed=3))
-    rec = lm.train(wl.pairs[:args.learned_train])
+    nvac = len(wl.vacua)
+    lm = LearnedPNAMP(wl, LearnedConfig(train_euler=256, epochs=30, seed=3, chunk=8))
+    step = max(1, len(wl.pairs) // max(1, args.learned_train))
+    train_pairs = wl.pairs[::step][:args.learned_train]
+    rec = lm.train(train_pairs)
     pts = len(wl.pairs) * lm.P * lm.G
 
     def timed(fn):
@@ -269,23 +282,27 @@ def learned_main(args):
         torch.cuda.synchronize()
         return out, time.perf_counter() - t0
 
+    (learned, gate), tl = timed(lambda: lm.run_gcm(wl.pairs, nvac))
+    timing = dict(lm.last_timing)
     exact, te = timed(lambda: lm.exact(wl.pairs))
-    learned, tl = timed(lambda: lm.run(wl.pairs))
-    base, tb = timed(lambda: lm.run(wl.pairs, use_net=False))
-    err = energy_errors_kev(learned, exact, nvac=len(wl.vacua), pairs=wl.pairs)
-    frac = sum(r["exact_euler"] for r in learned) / (len(learned) * lm.P)
-    print(json.dumps({
+    err = energy_errors_kev(learned, exact, nvac=nvac, pairs=wl.pairs)
+    out = {
         "metric": "projected kernel points/s, learned + mixed vs exact mixed (fine mesh)", "value": pts / tl,
         "unit": "points/s", "n_gpus": 1, "steps": 1, "warmup": 0, "ms_per_step": 1e3 * tl, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "df64+f32", "data": "synthetic: seeded vacua and TBMEs",
-        "config": {"workload": f"pf n=40, {len(wl.vacua)} vacua ({len(wl.pairs)} pairs), Euler 16x32x16 x gauge "
-                               f"11x11, coarse 4x8x4, network 4x256 trained on {args.learned_train} pairs"},
-        "exact_mixed": {"value": pts / te, "seconds": te},
-        "without_network": {"value": pts / tb, "seconds": tb,
-                            "exact_fraction": sum(r["exact_euler"] for r in base) / (len(base) * lm.P)},
-        "exact_fraction": frac, "fallback_pairs": sum(r["fallback"] for r in learned),
-        "timing_s": lm.last_timing, "training": rec,
-        "errors_keV": {k: v for k, v in err.items() if k != "per_pair_keV"}}))
+        "config": {"workload": f"pf n=40, {nvac} vacua ({len(wl.pairs)} pairs), Euler 16x32x16 x gauge "
+                               f"11x11, coarse 4x8x4, network 4x256 trained on {len(train_pairs)} pairs"},
+        "exact_mixed": {"value": pts / te, "seconds": te, "form": "df64"},
+        "speed_vs_exact_mixed": te / tl,
+        "exact_fraction": gate["exact_fraction"], "gate": gate,
+        "fallback_pairs": gate["fallback_pairs"], "timing_s": timing, "training": rec,
+        "errors_keV": {k: v for k, v in err.items() if k != "per_pair_keV"},
+        "gates_1keV": {"gcm_levels": err["gcm_levels_err_keV"] <= 1.0, "E_J": err["EJ_per_vacuum_err_keV"] <= 1.0}}
+    if args.learned_ablation:
+        base, tb = timed(lambda: lm.run(wl.pairs, use_net=False))
+        out["without_network"] = {"value": pts / tb, "seconds": tb,
+                                  "exact_fraction": sum(r["exact_euler"] for r in base) / (len(base) * lm.P)}
+    print(json.dumps(out))
     lm.close()
     return 0
 
@@ -432,8 +449,10 @@ def main():
                     help="pf: the 210-pair pf-shell set (headline); uneven: three model spaces in one launch; "
                          "learned: learned + mixed against exact mixed on a fine mesh; rho2b: the pf set with "
                          "the two-body transition density")
-    ap.add_argument("--learned-vacua", type=int, default=6)
-    ap.add_argument("--learned-train", type=int, default=10)
+    ap.add_argument("--learned-vacua", type=int, default=40)
+    ap.add_argument("--learned-train", type=int, default=200)
+    ap.add_argument("--learned-ablation", action="store_true",
+                    help="learned workload: also time the method without the network")
     ap.add_argument("--uneven-scale", type=int, default=1, help="divide the uneven batch's pair counts")
     ap.add_argument("--tune-scale", type=int, default=16,
                     help="the autotuner times schedules on the uneven batch divided by this")
@@ -664,7 +683,7 @@ def main():
                         "frac": fp32 / tf32 if tf32 else None,
                         "peak_source": "cuBLAS SGEMM 8192^3 measured in this run; achieved = FP64-equivalent "
                                        f"flops x {FP32_INSTR_PER_FLOP} FP32 instructions x 2 (FMA)",
-                        "traffic": TRAFFIC_BYTES_PER_POINT["df64"] * pts_step}
+                        "traffic": TRAFFIC_BYTES_PER_POINT["tc_point" if tc else "df64"] * pts_step}
         if tc:
             gf = gemm_flops_per_point(wl.sp)
             t_c = v["stage_ms_per_step"]["contract"] / 1e3
@@ -676,6 +695,7 @@ def main():
                 "bound": "tensor", "flops_per_point": gf, "achieved": achc, "peak": bf, "unit": "TFLOP/s",
                 "frac": achc / bf if achc and bf else None,
                 "executed_tflops": achc * nprod if achc else None,
+                "traffic": TRAFFIC_BYTES_PER_POINT["tc_contract"] * pts_step,
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (a kernel inside a long step)",
                 "note": f"algorithmic = one product of the dense group GEMMs; {form} executes {nprod}"}
 

@@ -85,6 +85,18 @@ int pnamp_learned_assemble(int npairs, int n_euler, int n_gauge, const double *g
                            const double *wts, double *zres, double *importance,
                            double *h_pred, void *stream);
 
+/* Coarse -> fine interpolation of per-gauge kernels, separable in the Euler angles.
+ * gc [npairs][cb][ca][cg][n_gauge][4] holds the coarse mesh's per-gauge output
+ * (N re, im, H/N re, im; Euler points beta outer, alpha, gamma inner, as
+ * pnamp_batch_items_device writes them); wb [fb][cb], wa [fa][ca], wg [fg][cg]
+ * are the 1-D interpolation weights (fine node x coarse node). Writes
+ * n_interp and h_interp [npairs][fb][fa][fg][n_gauge][2]:
+ * value(fb, fa, fg) = sum wb(fb, kb) wa(fa, ka) wg(fg, kg) value(kb, ka, kg).
+ * Needs ca cg n_gauge 32 bytes of shared memory (at most 227 KB). */
+int pnamp_learned_interp(int npairs, int cb, int ca, int cg, int fb, int fa, int fg, int n_gauge,
+                         const double *wb, const double *wa, const double *wg, const double *gc,
+                         double *h_interp, double *n_interp, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -118,6 +118,58 @@ __global__ void assemble_kernel(int npairs, int n_euler, int n_gauge, const doub
     }
 }
 
+// Coarse -> fine interpolation of the per-gauge coarse kernels, separable in the
+// three Euler angles: one block per (fine beta node, pair). The block first folds the
+// beta weights into T[ca][cg][g][4] (shared), then each output (fine alpha, fine gamma,
+// gauge point) takes sum_ca wa sum_cg wg T, gauge points innermost so the writes
+// are contiguous. Per output 4 x (cb + ca cg) multiply-adds instead of the cb ca cg of
+// the dense [P_fine x P_coarse] matrix product.
+__global__ void interp_kernel(int cb, int ca, int cg, int fb, int fa, int fg, int n_gauge,
+                              const double *__restrict__ wb, const double *__restrict__ wa,
+                              const double *__restrict__ wg, const double *__restrict__ gc,
+                              double *__restrict__ h_interp, double *__restrict__ n_interp) {
+    extern __shared__ double tsh[];          // [ca][cg][n_gauge][4]
+    const int ib = blockIdx.x, pr = blockIdx.y;
+    const long long pc = (long long)cb * ca * cg, pf = (long long)fb * fa * fg;
+    const double *src = gc + (long long)pr * pc * n_gauge * 4;
+    const int nt = ca * cg * n_gauge * 4;
+    for (int t = threadIdx.x; t < nt; t += blockDim.x) {
+        const int q = t & 3, g = (t >> 2) % n_gauge, ac = (t >> 2) / n_gauge;   // ac = ka cg + kg
+        double v = 0.0;
+        for (int kb = 0; kb < cb; ++kb)
+            v = fma(wb[ib * cb + kb], src[(((long long)kb * ca * cg + ac) * n_gauge + g) * 4 + q], v);
+        tsh[t] = v;
+    }
+    __syncthreads();
+    const int no = fa * fg * n_gauge;
+    double *ho = h_interp + ((long long)pr * pf + (long long)ib * fa * fg) * n_gauge * 2;
+    double *nout = n_interp + ((long long)pr * pf + (long long)ib * fa * fg) * n_gauge * 2;
+    for (int t = threadIdx.x; t < no; t += blockDim.x) {
+        const int g = t % n_gauge, ag = t / n_gauge, ja = ag / fg, jg = ag % fg;
+        double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+        for (int ka = 0; ka < ca; ++ka) {
+            double u0 = 0.0, u1 = 0.0, u2 = 0.0, u3 = 0.0;
+            for (int kg = 0; kg < cg; ++kg) {
+                const double w = wg[jg * cg + kg];
+                const double *tv = tsh + (((ka * cg + kg) * n_gauge + g) << 2);
+                u0 = fma(w, tv[0], u0);
+                u1 = fma(w, tv[1], u1);
+                u2 = fma(w, tv[2], u2);
+                u3 = fma(w, tv[3], u3);
+            }
+            const double w = wa[ja * ca + ka];
+            v0 = fma(w, u0, v0);
+            v1 = fma(w, u1, v1);
+            v2 = fma(w, u2, v2);
+            v3 = fma(w, u3, v3);
+        }
+        nout[2LL * t] = v0;
+        nout[2LL * t + 1] = v1;
+        ho[2LL * t] = v2;
+        ho[2LL * t + 1] = v3;
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -145,6 +197,23 @@ int pnamp_learned_assemble(int npairs, int n_euler, int n_gauge, const double *g
     if (npairs == 0) return 0;
     assemble_kernel<<<npairs * n_euler, 128, 0, (cudaStream_t)stream>>>(npairs, n_euler, n_gauge, gout, h_interp, out,
                                                                        scale, wts, zres, importance, h_pred);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
+}
+
+int pnamp_learned_interp(int npairs, int cb, int ca, int cg, int fb, int fa, int fg, int n_gauge, const double *wb,
+                         const double *wa, const double *wg, const double *gc, double *h_interp, double *n_interp,
+                         void *stream) {
+    if (npairs < 0 || cb < 1 || ca < 1 || cg < 1 || fb < 1 || fa < 1 || fg < 1 || n_gauge < 1 || !wb || !wa ||
+        !wg || !gc || !h_interp || !n_interp || fb > 65535 || npairs > 65535)
+        return 1;
+    const long long smem = (long long)ca * cg * n_gauge * 4 * sizeof(double);
+    if (smem > 227 * 1024) return 1;
+    if (npairs == 0) return 0;
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(interp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 2;
+    interp_kernel<<<dim3(fb, npairs), 256, (size_t)smem, (cudaStream_t)stream>>>(cb, ca, cg, fb, fa, fg, n_gauge, wb,
+                                                                                 wa, wg, gc, h_interp, n_interp);
     return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 

@@ -19,7 +19,14 @@ this mode instead
     `tol_kev` (0.5 keV) for any angular momentum that carries norm, the whole
     fine mesh of that pair is computed exactly (the fallback);
  6. projects N (exact) and H (exact where computed, N x predicted H/N
-    elsewhere) onto J, K1, K2 with the ordinary projection kernel.
+    elsewhere) onto J, K1, K2 with the ordinary projection kernel;
+ 7. (`run_gcm`, over the complete pair set of a GCM basis) the Hill-Wheeler
+    gate: with N^J exact for every pair, the norm matrix fixes HNDIAG's cutoff
+    subspace, and the first-order weight of each pair's H^J block on the lowest
+    GCM levels and on each vacuum's E_J follows from the Hill-Wheeler solutions
+    of the learned H^J (`gcm.level_weights`). Pairs are sent to the full mesh,
+    largest weight x estimated block error first, until the bound on the level
+    error left is below `gcm_safety` x `gcm_kev`.
 
 Errors are measured in the basis of normalised states: an error dH in
 H^J(q, q') is taken relative to sqrt(N^J(q, q) N^J(q', q')), the diagonal
@@ -80,11 +87,17 @@ def interp_poly(xc, xf):
     return L
 
 
-def interp_matrix(coarse: Mesh, fine: Mesh):
-    """[P_fine, P_coarse] weights in the Euler order beta outer, alpha, gamma inner."""
+def interp_factors(coarse: Mesh, fine: Mesh):
+    """The 1-D weights (wb, wa, wg), each [fine nodes, coarse nodes]."""
     ia = interp_periodic(coarse.alpha, fine.alpha)
     ig = interp_periodic(coarse.gamma, fine.gamma)
     ib = interp_poly(np.cos(coarse.beta[:coarse.nbet_used]), np.cos(fine.beta[:fine.nbet_used]))
+    return ib, ia, ig
+
+
+def interp_matrix(coarse: Mesh, fine: Mesh):
+    """[P_fine, P_coarse] weights in the Euler order beta outer, alpha, gamma inner."""
+    ib, ia, ig = interp_factors(coarse, fine)
     return np.kron(ib, np.kron(ia, ig))
 
 
@@ -104,6 +117,8 @@ class LearnedConfig:
     min_heldout: int = 32
     chunk: int = 4              # pairs per device batch
     rel_norm: float = 1e-3      # J checked when its diagonal-norm scale >= rel_norm x the largest
+    gcm_kev: float = 1.0        # Hill-Wheeler gate: bound on the GCM-level / E_J error left
+    gcm_safety: float = 0.5     # ... aimed at gcm_safety x gcm_kev
     seed: int = 0
 
 
@@ -123,7 +138,8 @@ class LearnedPNAMP:
         self.P, self.Pc, self.G = self.fine.n_euler, self.coarse.n_euler, fine.nfom ** 2
         self.euler = torch.from_numpy(fine.euler_points()).to(self.dev)          # [P, 4]
         self.wts = self.euler[:, 3].contiguous()
-        self.I = torch.from_numpy(interp_matrix(self.cmesh, fine)).to(self.dev)  # [P, Pc]
+        # separable interpolation weights (pnamp_learned_interp): beta, alpha, gamma
+        self.wi = [torch.from_numpy(np.ascontiguousarray(w)).to(self.dev) for w in interp_factors(self.cmesh, fine)]
         self.net = MLP(NF, self.cfg.width, self.cfg.depth, 3, seed=self.cfg.seed, device=self.dev)
         self.mean = torch.zeros(NF, dtype=torch.float32, device=self.dev)
         self.inv_std = torch.ones(NF, dtype=torch.float32, device=self.dev)
@@ -171,10 +187,14 @@ class LearnedPNAMP:
         Pc, G = self.Pc, self.G
         gc, zc, sc = self._buffers(npairs, Pc)
         self._run_items(self.coarse, uv, npairs, self._all_items(npairs, Pc), zc, sc, gc, "all")
-        h_i = torch.matmul(self.I, gc[..., 2:4].reshape(npairs, Pc, 2 * G)).reshape(npairs, self.P, G, 2)
-        n_i = torch.matmul(self.I, gc[..., 0:2].reshape(npairs, Pc, 2 * G)).reshape(npairs, self.P, G, 2)
+        h_i = torch.empty((npairs, self.P, G, 2), dtype=torch.float64, device=self.dev)
+        n_i = torch.empty_like(h_i)
+        wb, wa, wg = self.wi
+        (fb, cb), (fa, ca), (fg, cg) = wb.shape, wa.shape, wg.shape
+        _ck(_lib().pnamp_learned_interp(npairs, cb, ca, cg, fb, fa, fg, G, _p(wb), _p(wa), _p(wg), _p(gc),
+                                        _p(h_i), _p(n_i), self._stream()), "pnamp_learned_interp")
         nscale = torch.linalg.vector_norm(gc[..., 0:2], dim=-1).amax(dim=(1, 2))
-        return h_i.contiguous(), n_i.contiguous(), nscale.contiguous()
+        return h_i, n_i, nscale.contiguous()
 
     def features(self, npairs, deform, g, h_i, n_i, nscale, sel=None):
         nsel = 0 if sel is None else sel.shape[0]
@@ -415,6 +435,7 @@ class LearnedPNAMP:
                     rest = np.nonzero(~done)[0]
                     fb_sel.append(np.stack([np.full(len(rest), k), rest], 1))
                 info.append({"flagged": int(len(flagged[k])), "heldout": int(len(ho)), "est_err_keV": est_kev,
+                             "est_err_MeV": est,
                              "fallback": bool(fallback),
                              "heldout_err_rms": float(np.sqrt(np.mean(err_h[k][ho] ** 2))) if len(ho) else 0.0})
             if fb_sel:
@@ -432,9 +453,58 @@ class LearnedPNAMP:
         self.last_timing = tm
         return res
 
+    def run_gcm(self, pairs, nvac, jvals=(0, 2, 4, 6), eps=1e-5, nlev=3, exact_ctx=None):
+        """`run` over the complete pair set of `nvac` vacua, then the Hill-Wheeler gate.
+
+        Each pair's estimated H^J block error is (2J+1)^2 x its held-out estimate (the
+        spectral norm of a (2J+1)^2 block whose entries are each at most (2J+1) x the
+        Euler-summed error; 0 for pairs computed on the full mesh). The gate sends pairs
+        to the full mesh, the one with the largest weight x error first, until
+        max_J sum_pairs weight x error <= gcm_safety x gcm_kev, and recomputes them with
+        `exact_ctx` (a context of the fine mesh; None: this mode's own, in its form).
+        Returns (per-pair results, gate record)."""
+        from .gcm import level_weights
+        cfg = self.cfg
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = self.run(pairs)
+        t1 = time.perf_counter()
+        W = level_weights(res, pairs, nvac, jvals, eps, nlev)
+        est = np.array([0.0 if r["fallback"] else r["est_err_MeV"] for r in res])
+        err = {J: W[J] * (2 * J + 1) ** 2 * est for J in jvals}
+        bound = lambda: max(float(err[J].sum()) for J in jvals) * 1e3
+        b0 = bound()
+        target = cfg.gcm_safety * cfg.gcm_kev
+        gated = []
+        while bound() > target:
+            worst = max(jvals, key=lambda J: err[J].sum())
+            p = int(np.argmax(err[worst]))
+            if err[worst][p] == 0.0:
+                break
+            gated.append(p)
+            for J in jvals:
+                err[J][p] = 0.0
+        if gated:
+            gp = [pairs[p] for p in gated]
+            ex = self.exact(gp, ctx=exact_ctx)
+            for p, e in zip(gated, ex):
+                res[p]["hjkk"] = e["hjkk"]
+                res[p]["gated"] = True
+                res[p]["exact_euler"] = self.P
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        rec = {"bound_before_keV": b0, "bound_after_keV": bound(), "gated_pairs": len(gated),
+               "fallback_pairs": int(sum(r["fallback"] for r in res if not r.get("gated"))),
+               "run_s": t1 - t0, "gate_s": t2 - t1,
+               "exact_fraction": float(sum(r["exact_euler"] for r in res)) / (self.P * len(res))}
+        return res, rec
+
     # ------------------------------------------------------------------ the plain method
-    def exact(self, pairs):
-        """Every fine point exact (the plain quadrature) -> list of per-pair dicts (njkk, hjkk)."""
+    def exact(self, pairs, ctx=None):
+        """Every fine point exact (the plain quadrature) -> list of per-pair dicts (njkk, hjkk).
+
+        ctx: a context of the fine mesh to compute with (None: this mode's own)."""
+        ctx = ctx or self.fine
         out = []
         P = self.P
         for s in range(0, len(pairs), self.cfg.chunk):
@@ -443,7 +513,7 @@ class LearnedPNAMP:
             uv, _ = self._upload(chunk)
             z = torch.zeros((npairs, NOBS, P, 2), dtype=torch.float64, device=self.dev)
             st = torch.zeros((npairs, P), dtype=torch.int32, device=self.dev)
-            self.fine.batch_device(npairs, uv.data_ptr(), z.data_ptr(), st.data_ptr(), self._stream())
+            ctx.batch_device(npairs, uv.data_ptr(), z.data_ptr(), st.data_ptr(), self._stream())
             nj, hj = self.project(z, npairs)
             out += [{"pair": tuple(c), "njkk": nj[k], "hjkk": hj[k]} for k, c in enumerate(chunk)]
         return out

@@ -18,7 +18,7 @@ from .pnamp import load_library
 
 MLP_EXPORTS = ("pnamp_mlp_linear_forward", "pnamp_mlp_work_floats", "pnamp_mlp_linear_backward",
                "pnamp_mlp_loss_blocks", "pnamp_mlp_gauss_loss", "pnamp_mlp_adam", "pnamp_learned_features",
-               "pnamp_learned_assemble")
+               "pnamp_learned_assemble", "pnamp_learned_interp")
 
 _bound = False
 
@@ -37,6 +37,7 @@ def _lib():
         lib.pnamp_mlp_adam.argtypes = [vp, vp, vp, vp, C.c_longlong, f, f, f, f, i, vp]
         lib.pnamp_learned_features.argtypes = [i, i, i, vp, C.c_longlong] + [vp] * 10
         lib.pnamp_learned_assemble.argtypes = [i, i, i, vp, vp, vp, C.c_double, vp, vp, vp, vp, vp]
+        lib.pnamp_learned_interp.argtypes = [i] * 8 + [vp] * 7
         _bound = True
     return lib
 
