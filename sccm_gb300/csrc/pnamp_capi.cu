@@ -893,6 +893,12 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
     UP(jp_d, ot.jp_d);
     UP(jm_d, ot.jm_d);
     UP(mz_d, ot.mz_d);
+    {
+        const std::vector<dd> jj1_d = to_dd(jj1), t1b_d = to_dd(t1b_val), q_d = to_dd(q_val);
+        UP(jj1_d, ot.jj1_d);
+        UP(t1b_d, ot.t1b_val_d);
+        UP(q_d, ot.q_val_d);
+    }
     {   // one-body density blocks of ZRho1B_Angles (PNAMP_Rho1B.f90:14-29): states k1, k2 of the
         // same isospin, lj and m; it = 1 for protons (t = -1), 0 for neutrons; ordered it, lj, n1, n2
         // as Write_ME1B loops (PNAMP_Rho1B.f90:80-88)
@@ -925,6 +931,8 @@ int pnamp_init(const pnamp_space *sp, const pnamp_hamiltonian *h, const pnamp_me
         if (!idx.empty()) {
             UP(idx, ot.r1b_idx);
             UP(val, ot.r1b_val);
+            const std::vector<dd> val_d = to_dd(val);
+            UP(val_d, ot.r1b_val_d);
         }
         for (size_t e = 3; e < euler.size(); e += 4) c->euler_w.push_back(euler[e]);
         c->h_rec_idx.swap(h_rec_idx);

@@ -65,11 +65,13 @@ struct ObsTables {
     const double *mz;          // [n] m_a
     const double *jj1;         // [n] j(j+1)
     const dd *jp_d, *jm_d, *mz_d;   // the same coefficients as double-float
+    const dd *jj1_d, *t1b_val_d, *q_val_d;
     // one-body density blocks (t, lj, n1, n2) of ZRho1B_Angles: block b sums
     // r1b_val[e] rho(row, col) over e in [r1b_off[b], r1b_off[b + 1]), packed row*256+col
     int n_r1b;
     const int *r1b_off, *r1b_idx;
     const double *r1b_val;
+    const dd *r1b_val_d;
 };
 constexpr int kMaxR1B = 64;               // one-body density blocks per model space
 

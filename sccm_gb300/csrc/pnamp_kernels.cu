@@ -60,7 +60,9 @@ __device__ __forceinline__ zc sfms(zc a, zc b, zc c) { return zfms(a, b, c); }
 template <typename T> __device__ __forceinline__ T szero();
 template <> __device__ __forceinline__ double szero<double>() { return 0.0; }
 template <> __device__ __forceinline__ zc szero<zc>() { return mk(0.0, 0.0); }
-__device__ __forceinline__ double sabs1(zd a) { return (double)(fabsf(a.x.hi) + fabsf(a.y.hi)); }
+// pivot magnitude of a double-float value: the float sum of the high words, compared as a
+// float (the FP64 pipe is narrow on this part, and a float compares the same as its double)
+__device__ __forceinline__ float sabs1(zd a) { return fabsf(a.x.hi) + fabsf(a.y.hi); }
 __device__ __forceinline__ zd srecip(zd a) { return zrecip(a); }
 __device__ __forceinline__ zd smul(zd a, zd b) { return a * b; }
 __device__ __forceinline__ zd sfms(zd a, zd b, zd c) { return zfms(a, b, c); }
@@ -77,6 +79,15 @@ template <> struct Ar<zc> {
     static __device__ __forceinline__ R rmul(R a, R b) { return a * b; }
     static __device__ __forceinline__ bool nz(R a) { return a != 0.0; }
     static __device__ __forceinline__ R pick(const double *d, const dd *, long long i) { return d[i]; }
+    static __device__ __forceinline__ R rzero() { return 0.0; }
+    static __device__ __forceinline__ R radd(R a, R b) { return a + b; }
+    static __device__ __forceinline__ R rfma(R a, R b, R c) { return fma(a, b, c); }
+    static __device__ __forceinline__ double dbl(R a) { return a; }
+    static __device__ __forceinline__ R wsum(R v) {   // butterfly: the sum in every lane
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        return v;
+    }
     // pivot key: max(|re|, |im|) as the bit pattern of a non-negative double
     static __device__ __forceinline__ unsigned long long key(zc z) {
         const unsigned long long kx = (unsigned long long)__double_as_longlong(z.x) & 0x7fffffffffffffffull;
@@ -92,6 +103,16 @@ template <> struct Ar<zd> {
     static __device__ __forceinline__ R rmul(R a, R b) { return dd_mul(a, b); }
     static __device__ __forceinline__ bool nz(R a) { return a.hi != 0.0f; }
     static __device__ __forceinline__ R pick(const double *, const dd *f, long long i) { return f[i]; }
+    static __device__ __forceinline__ R rzero() { return dd_make(0.0f, 0.0f); }
+    static __device__ __forceinline__ R radd(R a, R b) { return dd_add(a, b); }
+    static __device__ __forceinline__ R rfma(R a, R b, R c) { return dd_fma(a, b, c); }
+    static __device__ __forceinline__ double dbl(R a) { return dd_to(a); }
+    static __device__ __forceinline__ R wsum(R v) {   // in double-float on the FP32 pipes
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            v = dd_add(v, dd_make(__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)));
+        return v;
+    }
     static __device__ __forceinline__ unsigned long long key(zd z) {
         const unsigned int kx = __float_as_uint(z.x.hi) & 0x7fffffffu;
         const unsigned int ky = __float_as_uint(z.y.hi) & 0x7fffffffu;
@@ -104,11 +125,12 @@ template <> struct Ar<zd> {
 // searches, the result is broadcast through sh[0] (row) and sh[1] (zero column).
 template <typename T>
 __device__ __forceinline__ int pivot_search(const T *A, int lda, int k, int n, int *sh, T *invd, bool &zero) {
+    using Mag = decltype(sabs1(A[0]));
     if (threadIdx.x < 32) {
-        double v = -1.0;
+        Mag v = -1;
         int idx = 0x7fffffff;
         for (int i = k + (int)threadIdx.x; i < n; i += 32) {
-            const double a = sabs1(A[i * lda + k]);
+            const Mag a = sabs1(A[i * lda + k]);
             if (a > v) {
                 v = a;
                 idx = i;
@@ -116,7 +138,7 @@ __device__ __forceinline__ int pivot_search(const T *A, int lda, int k, int n, i
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const double ov = __shfl_down_sync(0xffffffffu, v, o);
+            const Mag ov = __shfl_down_sync(0xffffffffu, v, o);
             const int oi = __shfl_down_sync(0xffffffffu, idx, o);
             if (ov > v || (ov == v && oi < idx)) {
                 v = ov;
@@ -126,7 +148,7 @@ __device__ __forceinline__ int pivot_search(const T *A, int lda, int k, int n, i
         if (threadIdx.x == 0) {
             // no comparable entry (all NaN): report a zero column, keep row k
             const bool none = (idx == 0x7fffffff);
-            const bool z = none || v == 0.0;
+            const bool z = none || v == Mag(0);
             sh[0] = none ? k : idx;
             sh[1] = z ? 1 : 0;
             invd[k] = z ? szero<T>() : srecip(A[(none ? k : idx) * lda + k]);
@@ -205,10 +227,11 @@ template <typename T>
 __device__ bool gj_right_solve(T *A, int n, T *Y, int ny, T *prow, T *pinv, int *sh) {
     const int lane = threadIdx.x & 31;
     auto search = [&](int k) {  // warp 0: pivot column of row k -> sh[0], zero flag sh[1], pinv[0]
-        double v = -1.0;
+        using Mag = decltype(sabs1(A[0]));
+        Mag v = -1;
         int idx = 0x7fffffff;
         for (int j = k + lane; j < n; j += 32) {
-            const double a = sabs1(A[k * n + j]);
+            const Mag a = sabs1(A[k * n + j]);
             if (a > v) {
                 v = a;
                 idx = j;
@@ -216,7 +239,7 @@ __device__ bool gj_right_solve(T *A, int n, T *Y, int ny, T *prow, T *pinv, int 
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const double ov = __shfl_down_sync(0xffffffffu, v, o);
+            const Mag ov = __shfl_down_sync(0xffffffffu, v, o);
             const int oi = __shfl_down_sync(0xffffffffu, idx, o);
             if (ov > v || (ov == v && oi < idx)) {
                 v = ov;
@@ -225,7 +248,7 @@ __device__ bool gj_right_solve(T *A, int n, T *Y, int ny, T *prow, T *pinv, int 
         }
         if (lane == 0) {
             const bool none = (idx == 0x7fffffff);  // all NaN: keep column k, report zero
-            const bool z = none || v == 0.0;
+            const bool z = none || v == Mag(0);
             sh[0] = none ? k : idx;
             sh[1] = z ? 1 : 0;
             pinv[0] = z ? szero<T>() : srecip(A[k * n + (none ? k : idx)]);
@@ -300,10 +323,11 @@ __device__ bool gj_right_solve_g(const Grp &g, T *A, int h, T *Y, int ny, T *pro
     const int hh = h * h, yh = ny * h;
     auto search = [&](int b, int k) {  // warp b: pivot column of row k of A_b
         const T *Ab = A + b * hh;
-        double v = -1.0;
+        using Mag = decltype(sabs1(A[0]));
+        Mag v = -1;
         int idx = 0x7fffffff;
         for (int j = k + lane; j < h; j += 32) {
-            const double a = sabs1(Ab[k * h + j]);
+            const Mag a = sabs1(Ab[k * h + j]);
             if (a > v) {
                 v = a;
                 idx = j;
@@ -311,7 +335,7 @@ __device__ bool gj_right_solve_g(const Grp &g, T *A, int h, T *Y, int ny, T *pro
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
-            const double ov = __shfl_down_sync(0xffffffffu, v, o);
+            const Mag ov = __shfl_down_sync(0xffffffffu, v, o);
             const int oi = __shfl_down_sync(0xffffffffu, idx, o);
             if (ov > v || (ov == v && oi < idx)) {
                 v = ov;
@@ -320,7 +344,7 @@ __device__ bool gj_right_solve_g(const Grp &g, T *A, int h, T *Y, int ny, T *pro
         }
         if (lane == 0) {
             const bool none = (idx == 0x7fffffff);
-            const bool z = none || v == 0.0;
+            const bool z = none || v == Mag(0);
             sh[2 * b] = none ? k : idx;
             sh[2 * b + 1] = z ? 1 : 0;
             pinv[b] = z ? szero<T>() : srecip(Ab[k * h + (none ? k : idx)]);
@@ -1239,88 +1263,95 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 // sums, spread over all warps, leave per-warp partials in red[kNSlot + ..].
                 // traces of rho, spread over warps 0 (species traces, sum j(j+1) rho_aa), 11 (J+, J-,
                 // Jz) and 12 (one-body energy) so that no warp starts the energy loop much later
+                // The sums run in the point arithmetic's real type R (double-float on the FP32
+                // pipes in that form) and leave it once per warp, in lane 0.
                 if (wid == 0 || wid == kNTrace + 1 || wid == kNTrace + 2) {
-                    double v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
+                    R v0 = A::rzero(), v1 = v0, v2 = v0, v3 = v0, v4 = v0, v5 = v0;
                     if (wid == 0) {
                         for (int a = lane; a < n; a += 32) {
-                            const zc d = A::to(rho[a * ld + a]);
-                            if (a < h) { v0 += d.x; v1 += d.y; }
-                            else { v2 += d.x; v3 += d.y; }
-                            v4 = fma(p.obs.jj1[a], d.x, v4);
-                            v5 = fma(p.obs.jj1[a], d.y, v5);
+                            const Z d = rho[a * ld + a];
+                            if (a < h) { v0 = A::radd(v0, d.x); v1 = A::radd(v1, d.y); }
+                            else { v2 = A::radd(v2, d.x); v3 = A::radd(v3, d.y); }
+                            const R jj = A::pick(p.obs.jj1, p.obs.jj1_d, a);
+                            v4 = A::rfma(jj, d.x, v4);
+                            v5 = A::rfma(jj, d.y, v5);
                         }
                     } else if (wid == kNTrace + 1) {
                         for (int a = lane; a < n; a += 32) {
-                            const double jpa = p.obs.jp[a], jma = p.obs.jm[a], mza = p.obs.mz[a];
-                            if (jpa != 0.0) {
-                                const zc r = A::to(rho[(a + 1) * ld + a]);
-                                v0 = fma(jpa, r.x, v0);
-                                v1 = fma(jpa, r.y, v1);
+                            const R jpa = A::pick(p.obs.jp, p.obs.jp_d, a), jma = A::pick(p.obs.jm, p.obs.jm_d, a);
+                            const R mza = A::pick(p.obs.mz, p.obs.mz_d, a);
+                            if (A::nz(jpa)) {
+                                const Z r = rho[(a + 1) * ld + a];
+                                v0 = A::rfma(jpa, r.x, v0);
+                                v1 = A::rfma(jpa, r.y, v1);
                             }
-                            if (jma != 0.0) {
-                                const zc r = A::to(rho[(a - 1) * ld + a]);
-                                v2 = fma(jma, r.x, v2);
-                                v3 = fma(jma, r.y, v3);
+                            if (A::nz(jma)) {
+                                const Z r = rho[(a - 1) * ld + a];
+                                v2 = A::rfma(jma, r.x, v2);
+                                v3 = A::rfma(jma, r.y, v3);
                             }
-                            const zc d = A::to(rho[a * ld + a]);
-                            v4 = fma(mza, d.x, v4);
-                            v5 = fma(mza, d.y, v5);
+                            const Z d = rho[a * ld + a];
+                            v4 = A::rfma(mza, d.x, v4);
+                            v5 = A::rfma(mza, d.y, v5);
                         }
                     } else {
                         for (int e = lane; e < p.obs.n_t1b; e += 32) {
                             const int ix = p.obs.t1b_idx[e];
-                            const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
-                            v0 = fma(p.obs.t1b_val[e], r.x, v0);
-                            v1 = fma(p.obs.t1b_val[e], r.y, v1);
+                            const Z r = rho[(ix >> 8) * ld + (ix & 255)];
+                            const R tv = A::pick(p.obs.t1b_val, p.obs.t1b_val_d, e);
+                            v0 = A::rfma(tv, r.x, v0);
+                            v1 = A::rfma(tv, r.y, v1);
                         }
                     }
                     // result slots: z 0,1  n 2,3  t1b 4,5  J+ 10,11  J- 12,13  Jz 14,15  j(j+1) 16,17
                     const int s0 = wid == 0 ? 0 : (wid == kNTrace + 1 ? 10 : 4);
                     const int cnt = wid == kNTrace + 2 ? 2 : 6;
-                    const double vals[6] = {v0, v1, v2, v3, v4, v5};
+                    const R vals[6] = {v0, v1, v2, v3, v4, v5};
 #pragma unroll
                     for (int q = 0; q < 6; ++q) {
                         if (q >= cnt) break;
-                        const double v = warp_sum(vals[q]);
+                        const R v = A::wsum(vals[q]);
                         const int slot = (wid == 0 && q >= 4) ? 12 + q : s0 + q;
-                        if (lane == 0) fin[slot] = v;
+                        if (lane == 0) fin[slot] = A::dbl(v);
                     }
                 } else if (p.iE2 && wid <= kNTrace) {  // Q_{2mu} traces: one warp per trace
                     const int q = wid - 1;
-                    double sr = 0.0, si = 0.0;
+                    R sr = A::rzero(), si = A::rzero();
                     for (int e = p.obs.q_off[q] + lane; e < p.obs.q_off[q + 1]; e += 32) {
                         const int ix = p.obs.q_idx[e];
-                        const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
-                        sr = fma(p.obs.q_val[e], r.x, sr);
-                        si = fma(p.obs.q_val[e], r.y, si);
+                        const Z r = rho[(ix >> 8) * ld + (ix & 255)];
+                        const R qv = A::pick(p.obs.q_val, p.obs.q_val_d, e);
+                        sr = A::rfma(qv, r.x, sr);
+                        si = A::rfma(qv, r.y, si);
                     }
-                    sr = warp_sum(sr);
-                    si = warp_sum(si);
+                    sr = A::wsum(sr);
+                    si = A::wsum(si);
                     if (lane == 0) {
-                        fin[18 + 2 * q] = sr;
-                        fin[19 + 2 * q] = si;
+                        fin[18 + 2 * q] = A::dbl(sr);
+                        fin[19 + 2 * q] = A::dbl(si);
                     }
                 }
                 if (r1out && wid > kNTrace) {  // one-body density blocks (ZRho1B_Angles): the idle warps
                     for (int b = wid - kNTrace - 1; b < p.obs.n_r1b; b += nw - kNTrace - 1) {
-                        double sr = 0.0, si = 0.0;
+                        R sr = A::rzero(), si = A::rzero();
                         for (int e = p.obs.r1b_off[b] + lane; e < p.obs.r1b_off[b + 1]; e += 32) {
                             const int ix = p.obs.r1b_idx[e];
-                            const zc r = A::to(rho[(ix >> 8) * ld + (ix & 255)]);
-                            sr = fma(p.obs.r1b_val[e], r.x, sr);
-                            si = fma(p.obs.r1b_val[e], r.y, si);
+                            const Z r = rho[(ix >> 8) * ld + (ix & 255)];
+                            const R bv = A::pick(p.obs.r1b_val, p.obs.r1b_val_d, e);
+                            sr = A::rfma(bv, r.x, sr);
+                            si = A::rfma(bv, r.y, si);
                         }
-                        sr = warp_sum(sr);
-                        si = warp_sum(si);
+                        sr = A::wsum(sr);
+                        si = A::wsum(si);
                         if (lane == 0) {
-                            red[kR1BSlot + 2 * b] = sr;
-                            red[kR1BSlot + 2 * b + 1] = si;
+                            red[kR1BSlot + 2 * b] = A::dbl(sr);
+                            red[kR1BSlot + 2 * b + 1] = A::dbl(si);
                         }
                     }
                 }
-                auto put = [&](int slot, double v) {  // slot 0..3: energy re/im, <J^2> re/im
-                    v = warp_sum(v);
-                    if (lane == 0) pw[slot * nw + wid] = v;
+                auto put = [&](int slot, R v) {  // slot 0..3: energy re/im, <J^2> re/im
+                    v = A::wsum(v);
+                    if (lane == 0) pw[slot * nw + wid] = A::dbl(v);
                 };
                 if (p.tc_splits) {
                     // tensor-core contraction: this gauge point's operand rows X[2 pt + ri] (rho
@@ -1357,8 +1388,10 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                             }
                         }
                     }
-                    put(0, 0.0);
-                    put(1, 0.0);
+                    if (lane == 0) {   // no energy sum in this form
+                        pw[wid] = 0.0;
+                        pw[nw + wid] = 0.0;
+                    }
                 } else {   // two-body energy, exact regrouping of the 8-term sum of
                     // PNAMP_Energy_OpenMP.f90:40-78:
                     // V[rho_ki rho_lj - rho_li rho_kj + d(rho_ik rho_jl - rho_jk rho_il)]
@@ -1408,9 +1441,8 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         rec_pn(pk0, v0);
                         if (two) rec_pn(pk1, v1);
                     }
-                    const zc e2c = A::to(e2);
-                    put(0, e2c.x);
-                    put(1, e2c.y);
+                    put(0, e2.x);
+                    put(1, e2.y);
                 }
                 {   // <J^2> (ZJ2_0, PNAMP_ME2B.f90:45-147) summed over x, y, z with
                     // Jx, Jy = (J+ +- J-)/(2, 2i):  sum_a j(j+1) rho_aa [above]
@@ -1439,9 +1471,8 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                             q = zfma(A::rmul(half, A::rmul(jma, jmc)) * k10[ac - ld], k01[ac - 1], q);
                         rest = rest + q;
                     }
-                    const zc rc = A::to(rest);
-                    put(2, rc.x);
-                    put(3, rc.y);
+                    put(2, rest.x);
+                    put(3, rest.y);
                 }
                 }  // !norm_only
                 __syncthreads();

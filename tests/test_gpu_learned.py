@@ -52,3 +52,30 @@ def test_network_gains_over_interpolation_alone(trained):
     rms_interp, rms_net = lm.validation_rms(wl.pairs[:10], n_euler=32)   # fresh Euler points
     print(f"H/N error at fresh points: interpolation {rms_interp:.4f} MeV, with the network {rms_net:.4f} MeV")
     assert rms_net < rms_interp
+
+
+def test_separable_interpolation_kernel_matches_dense_product():
+    """pnamp_learned_interp (three 1-D passes) against the dense [P_fine x P_coarse] product of
+    the same weights (np.kron), on random coarse per-gauge kernels."""
+    import torch
+    from sccm_gb300.learned import interp_factors, interp_matrix
+    from sccm_gb300.mlp import _ck, _lib, _p
+    coarse, fine, G, npairs = Mesh(4, 6, 4, 3), Mesh(8, 12, 8, 3), 9, 3
+    wb, wa, wg = interp_factors(coarse, fine)
+    I = interp_matrix(coarse, fine)
+    Pc, P = I.shape[1], I.shape[0]
+    rng = np.random.default_rng(5)
+    gc = rng.normal(size=(npairs, Pc, G, 4))
+    dev = torch.device("cuda")
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    h = torch.empty((npairs, P, G, 2), dtype=torch.float64, device=dev)
+    nn = torch.empty_like(h)
+    gcd, wbd, wad, wgd = t(gc), t(wb), t(wa), t(wg)
+    _ck(_lib().pnamp_learned_interp(npairs, wb.shape[1], wa.shape[1], wg.shape[1], wb.shape[0], wa.shape[0],
+                                    wg.shape[0], G, _p(wbd), _p(wad), _p(wgd), _p(gcd), _p(h), _p(nn),
+                                    torch.cuda.current_stream().cuda_stream), "pnamp_learned_interp")
+    torch.cuda.synchronize()
+    want = np.einsum("fc,pcgq->pfgq", I, gc)
+    scale = np.abs(want).max()
+    assert np.abs(nn.cpu().numpy() - want[..., 0:2]).max() <= 1e-12 * scale
+    assert np.abs(h.cpu().numpy() - want[..., 2:4]).max() <= 1e-12 * scale
