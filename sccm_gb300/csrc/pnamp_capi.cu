@@ -191,6 +191,7 @@ int plan_placement(Params &p, int smem_max) {
     pl.g_b = g; g += 2 * nn;
     pl.g_p = g; g += 4 * nn;
     pl.g_rw = g; g += nn;
+    pl.g_zr = g; g += nn;   // -Cscale Z0^-1 (reduced) or -Cscale Z0, in the point arithmetic
     pl.g_s = g; if (!pl.s_smem) g += s_elems;
     pl.g_t = g; if (!pl.t_smem) g += nn;
     pl.g_y = g; if (!pl.y_smem) g += 2 * nn;

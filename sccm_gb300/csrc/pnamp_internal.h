@@ -48,7 +48,7 @@ struct Placement {
     int off_s, off_t, off_y, off_uv;     // shared byte offsets (when *_smem)
     int off_piv, off_inv, off_red, off_rot, off_vec;
     int smem_bytes;
-    long long g_x, g_b, g_p, g_rw, g_s, g_t, g_y, g_uv;
+    long long g_x, g_b, g_p, g_rw, g_zr, g_s, g_t, g_y, g_uv;
     long long slot_elems;
 };
 

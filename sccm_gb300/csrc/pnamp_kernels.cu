@@ -480,6 +480,48 @@ __device__ __forceinline__ void exch_upper(Z *S, int N, int r, int p, int q) {
     __syncthreads();
 }
 
+// Running product of the Pfaffian's pivots. FP64 form: a complex double. Double-float
+// form: a double-float mantissa renormalised to [1/2, 1) in its largest part after every
+// factor, with the power of two kept as an integer, so that a product of many small or
+// large pivots neither leaves the float range nor needs the (narrow) FP64 pipe; one
+// conversion at the end.
+template <class Z> struct PfProd;
+template <> struct PfProd<zc> {
+    zc v = {1.0, 0.0};
+    __device__ __forceinline__ void mul(zc f, bool neg) { v = (neg ? -1.0 : 1.0) * (v * f); }
+    __device__ __forceinline__ zc get() const { return v; }
+};
+template <> struct PfProd<zd> {
+    zd m = {{1.0f, 0.0f}, {0.0f, 0.0f}};
+    int e = 0;
+    __device__ __forceinline__ void mul(zd f, bool neg) {
+        m = m * f;
+        if (neg) m = -m;
+        const float a = fmaxf(fabsf(m.x.hi), fabsf(m.y.hi));
+        if (a > 0.0f && a <= 3.0e38f) {
+            int ex;
+            frexpf(a, &ex);
+            m.x.hi = ldexpf(m.x.hi, -ex);
+            m.x.lo = ldexpf(m.x.lo, -ex);
+            m.y.hi = ldexpf(m.y.hi, -ex);
+            m.y.lo = ldexpf(m.y.lo, -ex);
+            e += ex;
+        }
+    }
+    __device__ __forceinline__ zc get() const {
+        const zc z = zd_to(m);
+        return mk(ldexp(z.x, e), ldexp(z.y, e));
+    }
+};
+// Pivot test of the Pfaffians: 0 fine, 1 |pivot| <= 1e-13 (the reference's exit), 2 not finite.
+__device__ __forceinline__ int pivot_flag(zc ss) { return !zfinite(ss) ? 2 : (!(abs2(ss) > 1.0e-26) ? 1 : 0); }
+__device__ __forceinline__ int pivot_flag(zd ss) {
+    if (!zfinite(ss)) return 2;
+    const float a = fabsf(ss.x.hi), b = fabsf(ss.y.hi);
+    // |ss|^2 > 1e-26 in float (the sum of squares underflows only far below the threshold)
+    return (a > 1.0e-13f || b > 1.0e-13f || a * a + b * b > 1.0e-26f) ? 0 : 1;
+}
+
 // Pfaffian of the N x N skew matrix in the upper triangle of S (row-major), the
 // 2x2-block elimination of ZPfaffianF (PNAMP_Proj.f90:218-350) with partial instead of
 // global pivoting: at each step the largest entry of row r right of the diagonal (first
@@ -493,7 +535,7 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &u
     // a one-warp search. (The reference's ZPfaffianF searches the whole remaining upper
     // triangle, PNAMP_Proj.f90:258-268; both are stable, results agree to rounding.)
     using A = Ar<Z>;
-    zc pf = mk(1.0, 0.0);  // running product, meaningful in thread 0
+    PfProd<Z> pf;  // running product, meaningful in thread 0
     underflow = 0;
     const int NB = N / 2;
     for (int k = 0; k < NB - 1; ++k) {
@@ -525,17 +567,16 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &u
             underflow = 2;
             return mk(0.0, 0.0);
         }
-        double phas = -1.0;  // the global-pivot sign rule with i1 = r (PNAMP_Proj.f90:273-275)
-        if (i2 == c) phas = -phas;
+        // the global-pivot sign rule with i1 = r (PNAMP_Proj.f90:273-275): -1, +1 without exchange
+        const bool neg = (i2 != c);
         if (i2 != c) exch_upper(S, N, r, c, i2);
         if (threadIdx.x == 0) {  // pivot test, reciprocal and running product by one thread
             const Z ssz = S[r * N + c];
-            const zc ss = A::to(ssz);
-            const int f = !zfinite(ss) ? 2 : (!(abs2(ss) > 1.0e-26) ? 1 : 0);
+            const int f = pivot_flag(ssz);
             flag[0] = f;
             if (f == 0) {
                 vec[c] = zrecip(ssz);
-                pf = phas * (pf * ss);
+                pf.mul(ssz, neg);
             }
         }
         __syncthreads();
@@ -560,9 +601,9 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &u
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) pf = pf * A::to(S[(N - 2) * N + N - 1]);
+    if (threadIdx.x == 0) pf.mul(S[(N - 2) * N + N - 1], false);
     __syncthreads();
-    return pf;
+    return threadIdx.x == 0 ? pf.get() : mk(0.0, 0.0);
 }
 
 // Pfaffians of two independent skew h x h matrices stored compactly (upper triangles,
@@ -585,7 +626,7 @@ __device__ zc pfaffian_upper_g(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fl
     const int lane = g.tid & 31, wid = g.wid;
     const int hh = h * h;
     const int nstep = h / 2 - 1;
-    zc pf = mk(1.0, 0.0);
+    PfProd<Z> pf;
     int uf = 0;
     // warp b: pivot of row r of matrix b over columns c..h-1 -> flag[b] (index), flag[2 + b]
     // (0 fine, 1 small, 2 non-finite), pv[b] (value), pv[2 + b] (reciprocal)
@@ -612,8 +653,7 @@ __device__ zc pfaffian_upper_g(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fl
         if (lane == 0) {
             const int q = (bidx == 0x7fffffff) ? r + 1 : bidx;  // at least one candidate when r + 1 < h
             const Z ssz = Sb[r * h + q];
-            const zc ss = A::to(ssz);
-            const int f = (bidx == 0x7fffffff || !zfinite(ss)) ? 2 : (!(abs2(ss) > 1.0e-26) ? 1 : 0);
+            const int f = (bidx == 0x7fffffff) ? 2 : pivot_flag(ssz);
             flag[b] = q;
             flag[2 + b] = f;
             pv[b] = ssz;
@@ -628,10 +668,7 @@ __device__ zc pfaffian_upper_g(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fl
         if (g.tid == 0) {
             const int fk = (NB > 1 && flag[3] > flag[2]) ? flag[3] : flag[2];
             if (uf == 0) uf = fk;  // the first failing step decides, as the early return did
-            for (int b = 0; b < NB; ++b) {
-                const double phas = ((b ? q1 : q0) == c) ? 1.0 : -1.0;
-                pf = phas * (pf * A::to(pv[b]));
-            }
+            for (int b = 0; b < NB; ++b) pf.mul(pv[b], (b ? q1 : q0) != c);
         }
         // (a) exchange c <-> q (exch_upper on every matrix) and v_i = S'[c][i] / S'[r][c], i > c
         for (int t = g.tid; t < NB * (h - r); t += g.nthr) {
@@ -699,13 +736,14 @@ __device__ zc pfaffian_upper_g(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fl
         }
         gsync(g);
     }
+    zc out = mk(0.0, 0.0);
     if (g.tid == 0) {
-        pf = pf * A::to(S[(h - 2) * h + h - 1]);
-        if (NB > 1) pf = pf * A::to(S[hh + (h - 2) * h + h - 1]);
-        if (uf) pf = mk(0.0, 0.0);
+        pf.mul(S[(h - 2) * h + h - 1], false);
+        if (NB > 1) pf.mul(S[hh + (h - 2) * h + h - 1], false);
+        if (!uf) out = pf.get();
     }
     underflow = uf;
-    return pf;
+    return out;
 }
 
 // ------------------------------------------------------------------ setup
@@ -848,6 +886,7 @@ cudaError_t launch_setup(const Params &p, int npairs, const double *uv, double *
 }
 
 // ------------------------------------------------------------------ points
+static_assert(sizeof(dd) == sizeof(double), "per-warp double-float partials share the double slots of red");
 constexpr int kNSlot = 36;  // observable sums: slots 0..37 final values, then per-warp partials
 constexpr int kR1BSlot = 128;  // one-body density block sums: red[kR1BSlot + 2b], re and im
 constexpr int kR2Norm = 260;   // the gauge point's norm, re and im, for the two-body density pass
@@ -883,6 +922,9 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
     zc *Bz = slot + pl.g_b;                         // the same storage while it holds FP64 values
     Z *P = reinterpret_cast<Z *>(slot + pl.g_p);    // T22 partials: V0p, V0n, U0p, U0n
     zc *RW = slot + pl.g_rw;                        // R W
+    // -Cscale Z0^-1 (reduced pairs) or -Cscale Z0: the constant block of the Pfaffian matrix,
+    // converted once per pair so that building S takes no FP64 work per gauge point
+    Z *CZ = reinterpret_cast<Z *>(slot + pl.g_zr);
     Z *S = reinterpret_cast<Z *>(pl.s_smem ? (void *)(smem + pl.off_s) : (void *)(slot + pl.g_s));
     Z *T = reinterpret_cast<Z *>(pl.t_smem ? (void *)(smem + pl.off_t) : (void *)(slot + pl.g_t));
     Z *Y = reinterpret_cast<Z *>(pl.y_smem ? (void *)(smem + pl.off_y) : (void *)(slot + pl.g_y));
@@ -937,6 +979,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 const int k = t / n, j = t % n;
                 V0t[t] = A::real(gV0[j * n + k]);
                 U0t[t] = A::real(gU0[j * n + k]);
+                CZ[t] = A::from(mk(-p.cscale * (reduced ? gZi[t] : gZ0[t]), 0.0));
             }
             for (int l = threadIdx.x; l < p.nfom; l += blockDim.x) {
                 const zc e = expi(p.nfom == 1 ? 0.0 : twopi * l / p.nfom);
@@ -1048,7 +1091,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                             int i, j;
                             tri_index(t, n, i, j);
                             const Z dd_ = (j < h) ? dpp : ((i < h) ? dpn : dnn);
-                            S[i * n + j] = X[i * n + j] * dd_ + A::from(mk(-p.cscale * gZi[i * n + j], 0.0));
+                            S[i * n + j] = X[i * n + j] * dd_ + CZ[i * n + j];
                         }
                         gsync(g);
                         pf = pfaffian_upper_g<Z, 1>(g, S, n, vec, reinterpret_cast<Z *>(red + kPfScratch), sh, under);
@@ -1082,7 +1125,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                             tri_index(t - b * Th, h, i, j);
                             const int gi = b * h + i, gj = b * h + j;
                             Z v = X[gi * n + gj] * (b ? dnn : dpp);
-                            v = v + A::from(mk(-p.cscale * gZi[gi * n + gj], 0.0));
+                            v = v + CZ[gi * n + gj];
                             S[b * h * h + i * h + j] = v;
                         }
                         gsync(g);
@@ -1119,11 +1162,11 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     if (j < n) {
                         const Z dd_ = (j < h) ? dpp : ((i < h) ? dpn : dnn);
                         v = X[i * n + j] * dd_;
-                        if (reduced) v = v + A::from(mk(-p.cscale * gZi[i * n + j], 0.0));
+                        if (reduced) v = v + CZ[i * n + j];
                     } else if (i < n) {
                         v = (j - n == i) ? mcs : zero;
                     } else {
-                        v = A::from(mk(-p.cscale * gZ0[(i - n) * n + (j - n)], 0.0));
+                        v = CZ[(i - n) * n + (j - n)];
                     }
                     S[i * NP + j] = v;
                 }
@@ -1163,7 +1206,10 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     pf = pfaffian_upper<Z>(S, NP, vec, red, sh + 2, under);
                     if (reduced) pf = pf * pfz;  // meaningful in thread 0, like pf
                 }
-                double *fin = red, *pw = red + kNSlot + 2;
+                // fin: final sums (double); pwR: per-warp energy and <J^2> partials in R (8 bytes,
+                // like a double, in both forms)
+                double *fin = red;
+                R *pwR = reinterpret_cast<R *>(red + kNSlot + 2);
                 if (!p.norm_only) {  // uniform over the block: norm-only launches skip the densities
                 // ---- T22(phi) and right-hand sides
                 if (split) {  // compact species blocks: T_b (h x h), Y_b = [R V1; R* U1] rows and columns of b
@@ -1351,7 +1397,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 }
                 auto put = [&](int slot, R v) {  // slot 0..3: energy re/im, <J^2> re/im
                     v = A::wsum(v);
-                    if (lane == 0) pw[slot * nw + wid] = A::dbl(v);
+                    if (lane == 0) pwR[slot * nw + wid] = v;
                 };
                 if (p.tc_splits) {
                     // tensor-core contraction: this gauge point's operand rows X[2 pt + ri] (rho
@@ -1389,8 +1435,8 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         }
                     }
                     if (lane == 0) {   // no energy sum in this form
-                        pw[wid] = 0.0;
-                        pw[nw + wid] = 0.0;
+                        pwR[wid] = A::rzero();
+                        pwR[nw + wid] = A::rzero();
                     }
                 } else {   // two-body energy, exact regrouping of the 8-term sum of
                     // PNAMP_Energy_OpenMP.f90:40-78:
@@ -1477,25 +1523,41 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 }  // !norm_only
                 __syncthreads();
                 if (wid == 0) {  // accumulation over the gauge points: warp 0, one observable per lane
+                    // The FP64 pipe is narrow on this part and its cost grows with the active lanes,
+                    // so each FP64 value is formed by the one lane that needs it: the norm by lane
+                    // 0 (then broadcast), H/N by lane 6 (and 0 for the per-gauge output), <J^2> by
+                    // lane 7; the per-warp energy and <J^2> partials are summed in the point
+                    // arithmetic first.
                     const unsigned full = 0xffffffffu;
-                    const zc pfv = mk(__shfl_sync(full, pf.x, 0), __shfl_sync(full, pf.y, 0));  // valid in lane 0
-                    double wsum[4];  // energy re/im, <J^2> re/im: per-warp partials summed
+                    R ws[4];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) wsum[q] = warp_sum(lane < nw ? pw[q * nw + lane] : 0.0);
-                    auto get = [&](int slot) { return (slot >= 6 && slot <= 9) ? wsum[slot - 6] : fin[slot]; };
-                    const zc zph = mk(p.gphase[2 * (lp * p.nfom + ln)], p.gphase[2 * (lp * p.nfom + ln) + 1]);
-                    const zc norm = onishi ? pfv : (p.vacfac * det0 * det1) * (pfv * zph);
-                    const zc trp = mk(get(10), get(11)), trm = mk(get(12), get(13)), trz = mk(get(14), get(15));
-                    const zc j2 = mk(get(16) + get(8), get(17) + get(9)) + trp * trm + trz * trz;
-                    const zc ekin = mk(get(4), get(5));
-                    zc hg = mk(0.0, 0.0);  // H/N at this gauge point (0 when not computed)
-                    if (!p.norm_only && !sing) hg = ekin + mk(get(6), get(7)) + mk(p.e0, 0.0);
+                    for (int q = 0; q < 4; ++q) ws[q] = A::wsum(lane < nw ? pwR[q * nw + lane] : A::rzero());
+                    const bool eval = !p.norm_only && !sing;
+                    zc norm = mk(0.0, 0.0);
+                    if (lane == 0) {
+                        const zc zph = mk(p.gphase[2 * (lp * p.nfom + ln)], p.gphase[2 * (lp * p.nfom + ln) + 1]);
+                        norm = onishi ? pf : (p.vacfac * det0 * det1) * (pf * zph);
+                    }
+                    norm.x = __shfl_sync(full, norm.x, 0);
+                    norm.y = __shfl_sync(full, norm.y, 0);
+                    zc o = mk(0.0, 0.0), hg = mk(0.0, 0.0);   // hg: H/N at this gauge point (0 if not computed)
+                    bool use = eval;
+                    if ((lane == 6 || (lane == 0 && gout)) && eval)
+                        hg = mk(fin[4] + A::dbl(ws[0]) + p.e0, fin[5] + A::dbl(ws[1]));
+                    if (lane == 1) o = mk(fin[0], fin[1]);
+                    else if (lane == 2) o = mk(fin[2], fin[3]);
+                    else if (lane == 3) o = mk(fin[4], fin[5]);      // one-body energy
+                    else if (lane == 6) o = hg;
+                    else if (lane == 7) {
+                        const zc trp = mk(fin[10], fin[11]), trm = mk(fin[12], fin[13]), trz = mk(fin[14], fin[15]);
+                        o = mk(fin[16] + A::dbl(ws[2]), fin[17] + A::dbl(ws[3])) + trp * trm + trz * trz;
+                    } else if (lane >= 8 && lane < 18 && p.iE2) o = mk(fin[2 * lane + 2], fin[2 * lane + 3]);  // Q slots 18..37
+                    else use = false;
                     if (p.tc_splits && lane == 0) {   // w = N / NFOM^2 of this gauge point, 0 if not evaluated
                         const long long pt = pt0 + lp * p.nfom + ln;
                         const double inv = 1.0 / ((double)p.nfom * p.nfom);
-                        const bool use = !p.norm_only && !sing;
-                        p.tc_w[2 * pt] = use ? inv * norm.x : 0.0;
-                        p.tc_w[2 * pt + 1] = use ? inv * norm.y : 0.0;
+                        p.tc_w[2 * pt] = eval ? inv * norm.x : 0.0;
+                        p.tc_w[2 * pt + 1] = eval ? inv * norm.y : 0.0;
                     }
                     if (lane == 0) {
                         acc[0] = acc[0] + norm;
@@ -1514,22 +1576,17 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         if (!p.norm_only && sing) f |= 2;
                         flags |= f;
                     }
-                    if (!p.norm_only && !sing) {
-                        zc o = mk(0.0, 0.0);
-                        bool use = true;
-                        if (lane == 1) o = mk(get(0), get(1));
-                        else if (lane == 2) o = mk(get(2), get(3));
-                        else if (lane == 3) o = ekin;
-                        else if (lane == 6) o = hg;
-                        else if (lane == 7) o = j2;
-                        else if (lane >= 8 && lane < 18 && p.iE2) o = mk(fin[2 * lane + 2], fin[2 * lane + 3]);  // Q slots 18..37
-                        else use = false;
-                        if (use) acc[lane] = zfma(norm, o, acc[lane]);
+                    if (use) acc[lane] = zfma(norm, o, acc[lane]);
+                    if (eval)
                         for (int b = lane; b < (r1out ? p.obs.n_r1b : 0); b += 32)
                             acc_r1b[b] = zfma(norm, mk(red[kR1BSlot + 2 * b], red[kR1BSlot + 2 * b + 1]), acc_r1b[b]);
-                    }
+                    __syncwarp();   // thread 0 reads every lane's accumulator after the last gauge point
                 }
-                __syncthreads();
+                // No CTA barrier here: the other warps go on to the next gauge point while warp 0
+                // accumulates this one. What warp 0 reads (the sums in red, pf, sing) is written
+                // again only after the next point's first CTA-wide barrier, which waits for warp 0;
+                // the two-body density pass reads the densities, so it keeps the barrier.
+                if (r2out) __syncthreads();
                 if (r2out && !p.norm_only && !sing) {
                     // ZRho2B_Angles (PNAMP_Rho2B.f90:105-112) before its Clebsch-Gordan sums:
                     // N [ZRO(k,i) ZRO(l,j) - ZRO(l,i) ZRO(k,j) + ZKAPA01(i,j) ZKAPA10(k,l)] per quadruple,
