@@ -18,7 +18,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libpnamp_gb300.so")
-SOURCES = ["pnamp_kernels.cu", "pnamp_capi.cu", "contract_tc.cu", "mlp_kernels.cu", "learned_kernels.cu"]
+SOURCES = ["pnamp_kernels.cu", "pnamp_capi.cu", "contract_tc.cu", "mlp_kernels.cu", "learned_kernels.cu", "hw_kernels.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -160,7 +160,7 @@ int plan_placement(Params &p, int smem_max) {
     Placement &pl = p.place;
     auto align = [](int x) { return (x + 15) & ~15; };
     // fixed shared pieces
-    int fixed = 0;
+    int fixed = 0, fixed2 = 0;
     pl.off_piv = fixed; fixed += align((n + 8) * 4);
     pl.off_inv = fixed; fixed += align(n * 16);
     pl.off_red = fixed; fixed += align(40 * (kThreads / 32) * 8);  // 36 observable slots per warp
@@ -179,13 +179,24 @@ int plan_placement(Params &p, int smem_max) {
     auto total = [&]() { return fixed + flags[0] * bs + flags[1] * bt + flags[2] * by + flags[3] * buv; };
     for (int k = 0; k < 4 && total() > smem_max; ++k) flags[order[k]] = 0;
     if (total() > smem_max) return PNAMP_ERR_UNSUPPORTED;
+    // species-split pairs with two gauge points in flight: after the fixed pieces, the compact
+    // V0^T / U0^T diagonal blocks and two half regions, when they fit (pf: 213 KB)
+    {
+        const int h = n / 2;
+        const int uvc = align(4 * h * h * 8);
+        const long long need = (long long)align(fixed) + uvc + 2LL * half_layout(h).bytes;
+        pl.sp2 = need <= smem_max ? 1 : 0;
+        pl.off_uvc = align(fixed);
+        pl.off_half = pl.off_uvc + uvc;
+        if (pl.sp2) fixed2 = (int)need;
+    }
     int off = fixed;
     pl.s_smem = flags[0]; pl.t_smem = flags[1]; pl.y_smem = flags[2]; pl.uv_smem = flags[3];
     if (pl.s_smem) { pl.off_s = off; off += bs; }
     if (pl.t_smem) { pl.off_t = off; off += bt; }
     if (pl.y_smem) { pl.off_y = off; off += by; }
     if (pl.uv_smem) { pl.off_uv = off; off += buv; }
-    pl.smem_bytes = off;
+    pl.smem_bytes = std::max(off, fixed2);
     long long g = 0;
     pl.g_x = g; g += nn;
     pl.g_b = g; g += 2 * nn;

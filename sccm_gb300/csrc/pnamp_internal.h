@@ -47,10 +47,41 @@ struct Placement {
     int s_smem, t_smem, y_smem, uv_smem;
     int off_s, off_t, off_y, off_uv;     // shared byte offsets (when *_smem)
     int off_piv, off_inv, off_red, off_rot, off_vec;
+    // species-split pairs, two gauge points in flight (when sp2): compact V0^T, U0^T
+    // diagonal blocks at off_uvc, then the two halves' regions (half_layout) from off_half
+    int sp2, off_uvc, off_half;
     int smem_bytes;
     long long g_x, g_b, g_p, g_rw, g_zr, g_s, g_t, g_y, g_uv;
     long long slot_elems;
 };
+
+// One half's shared region for the species-split path with two gauge points in flight:
+// byte offsets of the compact densities (rho, kappa10, kappa01, K; each two h x (h + 1)
+// species blocks; the Pfaffian's two h x h blocks come first in the same storage), T22's
+// two blocks, the right-hand sides, the solve's pivot row, the Pfaffian vector and pivots,
+// the accumulators, the final sums, the per-warp partials and the flags.
+constexpr int kHalfThreads = kThreads / 2, kHalfWarps = kHalfThreads / 32;
+struct HalfLayout {
+    int dens, t, y, invd, vec, pfs, acc, fin, pw, sh, bytes;
+};
+__host__ __device__ inline HalfLayout half_layout(int h) {
+    constexpr int zs = 16;   // complex element, both arithmetics
+    HalfLayout L;
+    int o = 0;
+    auto take = [&](int bytes) { const int at = o; o += (bytes + 15) & ~15; return at; };
+    L.dens = take(8 * h * (h + 1) * zs);
+    L.t = take(2 * h * h * zs);
+    L.y = take(4 * h * h * zs);
+    L.invd = take(2 * h * zs);
+    L.vec = take((2 * h + 4) * zs);
+    L.pfs = take(4 * zs);
+    L.acc = take(kNobs * 16);
+    L.fin = take(40 * 8);
+    L.pw = take(4 * kHalfWarps * 8);
+    L.sh = take(16 * 4);
+    L.bytes = o;
+    return L;
+}
 
 // Sparse one-body data used by the observables, built on the host once.
 struct ObsTables {

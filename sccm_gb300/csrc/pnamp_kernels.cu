@@ -27,7 +27,10 @@
 //   kappa01 = -D* (R* U1 T22^-1) V0^T.
 #include <cuda_bf16.h>
 
+#include <type_traits>
+
 #include "pnamp_df64.cuh"
+#include "../../include/pnamp_gpu.h"
 #include "pnamp_internal.h"
 
 namespace pnamp {
@@ -80,6 +83,7 @@ template <> struct Ar<zc> {
     static __device__ __forceinline__ bool nz(R a) { return a != 0.0; }
     static __device__ __forceinline__ R pick(const double *d, const dd *, long long i) { return d[i]; }
     static __device__ __forceinline__ R rzero() { return 0.0; }
+    static __device__ __forceinline__ R rconst(float v) { return (double)v; }   // exact
     static __device__ __forceinline__ R radd(R a, R b) { return a + b; }
     static __device__ __forceinline__ R rfma(R a, R b, R c) { return fma(a, b, c); }
     static __device__ __forceinline__ double dbl(R a) { return a; }
@@ -104,6 +108,7 @@ template <> struct Ar<zd> {
     static __device__ __forceinline__ bool nz(R a) { return a.hi != 0.0f; }
     static __device__ __forceinline__ R pick(const double *, const dd *f, long long i) { return f[i]; }
     static __device__ __forceinline__ R rzero() { return dd_make(0.0f, 0.0f); }
+    static __device__ __forceinline__ R rconst(float v) { return dd_make(v, 0.0f); }   // exact
     static __device__ __forceinline__ R radd(R a, R b) { return dd_add(a, b); }
     static __device__ __forceinline__ R rfma(R a, R b, R c) { return dd_fma(a, b, c); }
     static __device__ __forceinline__ double dbl(R a) { return dd_to(a); }
@@ -202,6 +207,19 @@ __device__ bool lu_factor(T *A, int n, int lda, int *perm, T *invd, int *sh) {
     return sing;
 }
 
+// Warp argmax by one integer max-reduction (redux.sync): the key of candidate j (offset
+// jrel = j - j0 < 64) is the magnitude's bit pattern (a non-negative float compares like its
+// bits) with the low 6 bits replaced by 63 - jrel, so the largest magnitude wins and ties go
+// to the first column, magnitudes being compared to 2^-17 relative. Lanes pass their best key
+// (0 for no candidate). Returns the winning offset in bits 0..5 of the reduced key; the key's
+// magnitude part is 0 when every candidate was zero (or not a number, which counts as zero).
+__device__ __forceinline__ unsigned pack_key(float mag, int jrel) {
+    return (mag >= 0.0f ? (__float_as_uint(mag) & ~63u) : 0u) | (unsigned)(63 - jrel);
+}
+__device__ __forceinline__ unsigned pack_key_bits(unsigned bits, int jrel) { return (bits & ~63u) | (unsigned)(63 - jrel); }
+// the grouped eliminations search at most n <= PNAMP_MAX_NLEV candidates
+static_assert(PNAMP_MAX_NLEV <= 64, "pivot offsets are packed into 6 bits (7 for the 2n x 2n Pfaffian)");
+
 // A warp-aligned group of the CTA's threads with its own named barrier (bar.sync id,
 // count; id 0 with the whole CTA is __syncthreads). Lets two independent latency-bound
 // eliminations run at the same time on disjoint warps.
@@ -227,31 +245,47 @@ template <typename T>
 __device__ bool gj_right_solve(T *A, int n, T *Y, int ny, T *prow, T *pinv, int *sh) {
     const int lane = threadIdx.x & 31;
     auto search = [&](int k) {  // warp 0: pivot column of row k -> sh[0], zero flag sh[1], pinv[0]
-        using Mag = decltype(sabs1(A[0]));
-        Mag v = -1;
-        int idx = 0x7fffffff;
-        for (int j = k + lane; j < n; j += 32) {
-            const Mag a = sabs1(A[k * n + j]);
-            if (a > v) {
-                v = a;
-                idx = j;
+        if constexpr (std::is_same<T, zd>::value) {   // one redux.sync
+            unsigned key = 0u;
+            for (int j = k + lane; j < n; j += 32) {
+                const unsigned kk = pack_key(sabs1(A[k * n + j]), j - k);
+                key = key > kk ? key : kk;
             }
-        }
+            const unsigned m = __reduce_max_sync(0xffffffffu, key);
+            if (lane == 0) {
+                const int idx = k + 63 - (int)(m & 63u);
+                const bool z = (m >> 6) == 0u;
+                sh[0] = idx;
+                sh[1] = z ? 1 : 0;
+                pinv[0] = z ? szero<T>() : srecip(A[k * n + idx]);
+            }
+        } else {
+            using Mag = decltype(sabs1(A[0]));
+            Mag v = -1;
+            int idx = 0x7fffffff;
+            for (int j = k + lane; j < n; j += 32) {
+                const Mag a = sabs1(A[k * n + j]);
+                if (a > v) {
+                    v = a;
+                    idx = j;
+                }
+            }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const Mag ov = __shfl_down_sync(0xffffffffu, v, o);
-            const int oi = __shfl_down_sync(0xffffffffu, idx, o);
-            if (ov > v || (ov == v && oi < idx)) {
-                v = ov;
-                idx = oi;
+            for (int o = 16; o > 0; o >>= 1) {
+                const Mag ov = __shfl_down_sync(0xffffffffu, v, o);
+                const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+                if (ov > v || (ov == v && oi < idx)) {
+                    v = ov;
+                    idx = oi;
+                }
             }
-        }
-        if (lane == 0) {
-            const bool none = (idx == 0x7fffffff);  // all NaN: keep column k, report zero
-            const bool z = none || v == Mag(0);
-            sh[0] = none ? k : idx;
-            sh[1] = z ? 1 : 0;
-            pinv[0] = z ? szero<T>() : srecip(A[k * n + (none ? k : idx)]);
+            if (lane == 0) {
+                const bool none = (idx == 0x7fffffff);  // all NaN: keep column k, report zero
+                const bool z = none || v == Mag(0);
+                sh[0] = none ? k : idx;
+                sh[1] = z ? 1 : 0;
+                pinv[0] = z ? szero<T>() : srecip(A[k * n + (none ? k : idx)]);
+            }
         }
     };
     bool sing = false;
@@ -321,33 +355,52 @@ template <typename T, int NB = 2>
 __device__ bool gj_right_solve_g(const Grp &g, T *A, int h, T *Y, int ny, T *prow, T *pinv, int *sh) {
     const int lane = g.tid & 31, wid = g.wid;
     const int hh = h * h, yh = ny * h;
+    // The search of step k + 1 runs beside each step's updates, on its critical path, so in
+    // the double-float form it is one redux.sync; the FP64 form keeps the shuffle search.
+    constexpr bool kDF = std::is_same<T, zd>::value;
     auto search = [&](int b, int k) {  // warp b: pivot column of row k of A_b
         const T *Ab = A + b * hh;
-        using Mag = decltype(sabs1(A[0]));
-        Mag v = -1;
-        int idx = 0x7fffffff;
-        for (int j = k + lane; j < h; j += 32) {
-            const Mag a = sabs1(Ab[k * h + j]);
-            if (a > v) {
-                v = a;
-                idx = j;
+        if constexpr (kDF) {
+            unsigned key = 0u;
+            for (int j = k + lane; j < h; j += 32) {
+                const unsigned kk = pack_key(sabs1(Ab[k * h + j]), j - k);
+                key = key > kk ? key : kk;
             }
-        }
+            const unsigned m = __reduce_max_sync(0xffffffffu, key);
+            if (lane == 0) {
+                const int idx = k + 63 - (int)(m & 63u);
+                const bool z = (m >> 6) == 0u;
+                sh[2 * b] = idx;
+                sh[2 * b + 1] = z ? 1 : 0;
+                pinv[b] = z ? szero<T>() : srecip(Ab[k * h + idx]);
+            }
+        } else {
+            using Mag = decltype(sabs1(A[0]));
+            Mag v = -1;
+            int idx = 0x7fffffff;
+            for (int j = k + lane; j < h; j += 32) {
+                const Mag a = sabs1(Ab[k * h + j]);
+                if (a > v) {
+                    v = a;
+                    idx = j;
+                }
+            }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const Mag ov = __shfl_down_sync(0xffffffffu, v, o);
-            const int oi = __shfl_down_sync(0xffffffffu, idx, o);
-            if (ov > v || (ov == v && oi < idx)) {
-                v = ov;
-                idx = oi;
+            for (int o = 16; o > 0; o >>= 1) {
+                const Mag ov = __shfl_down_sync(0xffffffffu, v, o);
+                const int oi = __shfl_down_sync(0xffffffffu, idx, o);
+                if (ov > v || (ov == v && oi < idx)) {
+                    v = ov;
+                    idx = oi;
+                }
             }
-        }
-        if (lane == 0) {
-            const bool none = (idx == 0x7fffffff);
-            const bool z = none || v == Mag(0);
-            sh[2 * b] = none ? k : idx;
-            sh[2 * b + 1] = z ? 1 : 0;
-            pinv[b] = z ? szero<T>() : srecip(Ab[k * h + (none ? k : idx)]);
+            if (lane == 0) {
+                const bool none = (idx == 0x7fffffff);
+                const bool z = none || v == Mag(0);
+                sh[2 * b] = none ? k : idx;
+                sh[2 * b + 1] = z ? 1 : 0;
+                pinv[b] = z ? szero<T>() : srecip(Ab[k * h + (none ? k : idx)]);
+            }
         }
     };
     bool sing = false;
@@ -359,7 +412,6 @@ __device__ bool gj_right_solve_g(const Grp &g, T *A, int h, T *Y, int ny, T *pro
     for (int k = 0; k < h; ++k) {
         const int c0 = sh[0], c1 = NB > 1 ? sh[2] : 0;
         if (sh[1] || (NB > 1 && sh[3])) sing = true;
-        const T pv0 = pinv[0], pv1 = NB > 1 ? pinv[1] : pinv[0];
         // phase 1 (all systems): m_r = M[r][c] / A[k][c] into column k, old column k into
         // column c, the exchanged pivot row into prow
         const int nrT = h - k - 1, nrows = nrT + ny, per1 = nrows + h;
@@ -370,7 +422,7 @@ __device__ bool gj_right_solve_g(const Grp &g, T *A, int h, T *Y, int ny, T *pro
             if (u < nrows) {
                 T *row = u < nrT ? Ab + (k + 1 + u) * h : Y + b * yh + (u - nrT) * h;
                 const T a = row[c], bb = row[k];
-                row[k] = smul(a, b ? pv1 : pv0);
+                row[k] = smul(a, pinv[b]);
                 if (c != k) row[c] = bb;
             } else {
                 const int j = u - nrows;
@@ -527,7 +579,7 @@ __device__ __forceinline__ int pivot_flag(zd ss) {
 // global pivoting: at each step the largest entry of row r right of the diagonal (first
 // maximum; magnitude max(|re|,|im|)) is moved to (r, r+1), the sign flips once per
 // exchange, Pf = 0 when |pivot| <= 1e-13, and the Schur complement is updated in place.
-// The running product is kept in FP64. `vec` holds N scratch values; `flag` 2 ints.
+// The running product is a PfProd. `vec` holds N scratch values; `flag` 2 ints.
 template <class Z>
 __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &underflow) {
     // Parlett-Reid elimination with partial pivoting: step k takes the largest entry of
@@ -540,7 +592,17 @@ __device__ zc pfaffian_upper(Z *S, int N, Z *vec, double *red, int *flag, int &u
     const int NB = N / 2;
     for (int k = 0; k < NB - 1; ++k) {
         const int r = 2 * k, c = r + 1;
-        if (threadIdx.x < 32) {
+        if (std::is_same<Z, zd>::value && threadIdx.x < 32) {
+            // one redux.sync over keys with 7 offset bits (N = 2n <= 128 candidates; the
+            // high bits of the 31-bit magnitude key first, ties to the first column)
+            unsigned key = 0u;
+            for (int j = c + (int)threadIdx.x; j < N; j += 32) {
+                const unsigned kk = ((unsigned)A::key(S[r * N + j]) & ~127u) | (unsigned)(127 - (j - c));
+                key = key > kk ? key : kk;
+            }
+            const unsigned m = __reduce_max_sync(0xffffffffu, key);
+            if (threadIdx.x == 0) flag[1] = c + 127 - (int)(m & 127u);
+        } else if (threadIdx.x < 32) {
             unsigned long long best = 0ull;
             int bidx = 0x7fffffff;
             for (int j = c + (int)threadIdx.x; j < N; j += 32) {
@@ -632,6 +694,24 @@ __device__ zc pfaffian_upper_g(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fl
     // (0 fine, 1 small, 2 non-finite), pv[b] (value), pv[2 + b] (reciprocal)
     auto search = [&](int b, int r) {
         const Z *Sb = S + b * hh;
+        if constexpr (std::is_same<Z, zd>::value) {   // one redux.sync; candidates r + 1 .. h - 1 exist
+            unsigned key = 0u;
+            for (int j = r + 1 + lane; j < h; j += 32) {
+                const unsigned kk = pack_key_bits((unsigned)A::key(Sb[r * h + j]), j - r - 1);
+                key = key > kk ? key : kk;
+            }
+            const unsigned m = __reduce_max_sync(0xffffffffu, key);
+            if (lane == 0) {
+                const int q = r + 1 + 63 - (int)(m & 63u);
+                const Z ssz = Sb[r * h + q];
+                const int f = pivot_flag(ssz);
+                flag[b] = q;
+                flag[2 + b] = f;
+                pv[b] = ssz;
+                pv[2 + b] = f ? ssz : zrecip(ssz);
+            }
+            return;
+        }
         unsigned long long best = 0ull;
         int bidx = 0x7fffffff;
         for (int j = r + 1 + lane; j < h; j += 32) {
@@ -899,6 +979,373 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
+// ---- species-split pairs, two gauge points in flight --------------------------------------
+// The CTA's two halves (8 warps each) take alternate gauge points of the Euler point and run
+// them independently: in each half warps 0-1 eliminate the two species' Schur-complement
+// blocks while warps 2-7 solve the two T22 systems (named barriers 1 + 3 s and 2 + 3 s for
+// half s), and one half-wide barrier (3 + 3 s) separates the densities, K and the
+// observables; warp 0 of each half accumulates its gauge points. A step of one half that
+// waits on a barrier leaves the SM to the other half, which the single-point path (one CTA
+// of 16 warps per gauge point) cannot do. The densities are stored compactly, two h x (h + 1)
+// species blocks per density (the proton-neutron blocks of a split pair vanish). Thread 0
+// sums the halves' accumulators at the end.
+template <class Z>
+__device__ __forceinline__ void split_pair_points(const Params &p, unsigned char *smem, const Z *X, const Z *P,
+                                                  const Z *B, const Z *CZ, const Z *ephz, zc pfz, double det0,
+                                                  double det1, int pair, int ie, long long pt0, double *gout,
+                                                  double *zout, int *status) {
+    using A = Ar<Z>;
+    using R = typename A::R;
+    const int n = p.n, h = p.h, nn = n * n;
+    const int half = threadIdx.x / kHalfThreads, lt = threadIdx.x % kHalfThreads;
+    const int lane = lt & 31, lw = lt >> 5;
+    const HalfLayout L = half_layout(h);
+    unsigned char *hb = smem + p.place.off_half + half * L.bytes;
+    const int hl = h + 1, bs = h * hl, ds = 2 * bs, hh = h * h;   // compact row stride, block, density
+    Z *Dn = reinterpret_cast<Z *>(hb + L.dens);
+    Z *rhoC = Dn, *k10C = Dn + ds, *k01C = Dn + 2 * ds, *KcC = Dn + 3 * ds;
+    Z *S2 = Dn;
+    Z *T2 = reinterpret_cast<Z *>(hb + L.t), *Y2 = reinterpret_cast<Z *>(hb + L.y);
+    Z *inv2 = reinterpret_cast<Z *>(hb + L.invd), *vec2 = reinterpret_cast<Z *>(hb + L.vec);
+    Z *pfs2 = reinterpret_cast<Z *>(hb + L.pfs);
+    zc *acc2 = reinterpret_cast<zc *>(hb + L.acc);
+    double *fin2 = reinterpret_cast<double *>(hb + L.fin);
+    R *pw2 = reinterpret_cast<R *>(hb + L.pw);
+    int *sh2 = reinterpret_cast<int *>(hb + L.sh);   // [0, 4) Pfaffian, [4, 8) solve, [8] flags
+    // compact V0^T, U0^T: species b, [b][k][j] = V0(b h + j, b h + k)
+    const R *V0c = reinterpret_cast<const R *>(smem + p.place.off_uvc), *U0c = V0c + 2 * hh;
+    const int barH = 3 + 3 * half;
+    auto hsync = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(barH), "r"(kHalfThreads) : "memory"); };
+    // compact index of (r, c), r and c of the same species
+    auto cidx = [&](int r, int c) {
+        const int b = r >= h ? 1 : 0;
+        return b * bs + (r - b * h) * hl + (c - b * h);
+    };
+    const Z zero = A::from(mk(0.0, 0.0));
+    const Z csz = A::from(mk(p.cscale, 0.0));
+    for (int io = lt; io < kNobs; io += kHalfThreads) acc2[io] = mk(0.0, 0.0);
+    if (lt == 0) sh2[8] = 0;
+    hsync();
+    for (int gi = half; gi < p.n_gauge; gi += 2) {
+        const int lp = gi / p.nfom, ln = gi % p.nfom;
+        const Z zep = ephz[lp], zepc = zconj(zep), zen = ephz[ln], zenc = zconj(zen);
+        const Z dpp = csz * (zep * zep), dnn = csz * (zen * zen);
+        int under = 0;
+        zc pf = mk(0.0, 0.0);
+        bool sing = false;
+        if (lw < 2) {   // the two species' Schur-complement blocks and their Pfaffians
+            const Grp g{lt, 64, lw, 1 + 3 * half};
+            const int Th = h * (h - 1) / 2;
+            for (int t = g.tid; t < 2 * Th; t += g.nthr) {
+                const int b = t >= Th ? 1 : 0;
+                int i, j;
+                tri_index(t - b * Th, h, i, j);
+                const int gi_ = b * h + i, gj_ = b * h + j;
+                S2[b * hh + i * h + j] = X[gi_ * n + gj_] * (b ? dnn : dpp) + CZ[gi_ * n + gj_];
+            }
+            gsync(g);
+            pf = pfaffian_upper_g<Z, 2>(g, S2, h, vec2, pfs2, sh2, under);
+            pf = pf * pfz;   // meaningful in the half's thread 0
+        } else if (!p.norm_only) {   // T22 blocks, right-hand sides, Y T22^-1
+            const Grp g{lt - 64, kHalfThreads - 64, lw - 2, 2 + 3 * half};
+            for (int t = g.tid; t < 2 * hh; t += g.nthr) {
+                const int b = t >= hh ? 1 : 0, e = t - b * hh, i = e / h, j = e % h;
+                const int gg = (b * h + i) * n + b * h + j;
+                Z sv = zep * P[gg];
+                sv = zfma(zen, P[nn + gg], sv);
+                sv = zfma(zepc, P[2 * nn + gg], sv);
+                sv = zfma(zenc, P[3 * nn + gg], sv);
+                T2[t] = sv;
+            }
+            for (int t = g.tid; t < 4 * hh; t += g.nthr) {
+                const int b = t >= 2 * hh ? 1 : 0, e = t - 2 * b * hh, r = e / h, j = e % h;
+                const int grow = r < h ? b * h + r : n + b * h + (r - h);
+                Y2[t] = B[grow * n + b * h + j];
+            }
+            gsync(g);
+            const bool sg = gj_right_solve_g<Z, 2>(g, T2, h, Y2, 2 * h, inv2, vec2 + 2 * h, sh2 + 4);
+            if (g.tid == 0) sh2[4] = sg ? 1 : 0;
+        }
+        hsync();
+        if (!p.norm_only) sing = sh2[4] != 0;
+        if (!p.norm_only) {
+            // ---- densities of each species block (rho, kappa10, kappa01 share the loads)
+            for (int t = lt; t < 2 * hh; t += kHalfThreads) {
+                const int b = t >= hh ? 1 : 0, e = t - b * hh, i = e / h, j = e % h;
+                const Z *Yt = Y2 + 2 * b * hh + i * h;
+                const Z *Yb = Yt + hh;
+                const R *Mv = V0c + b * hh + j, *Mu = U0c + b * hh + j;
+                Z sr = zero, s10 = zero, s01 = zero;
+                for (int k = 0; k < h; ++k) {
+                    const Z yt = Yt[k];
+                    const R mv = Mv[k * h];
+                    sr = rfma(mv, yt, sr);
+                    s10 = rfma(Mu[k * h], yt, s10);
+                    s01 = rfma(mv, Yb[k], s01);
+                }
+                const Z di = b ? zen : zep;
+                const int o = b * bs + i * hl + j;
+                rhoC[o] = di * sr;
+                k10C[o] = di * s10;
+                k01C[o] = -(zconj(di) * s01);
+            }
+            hsync();
+            // ---- K01_ij (i < j) at K[i][j], K10_ij at K[j][i], within each block
+            {
+                const int Th = h * (h - 1) / 2;
+                for (int t = lt; t < 2 * Th; t += kHalfThreads) {
+                    const int b = t >= Th ? 1 : 0;
+                    int i, j;
+                    tri_index(t - b * Th, h, i, j);
+                    const int oij = b * bs + i * hl + j, oji = b * bs + j * hl + i;
+                    KcC[oij] = k01C[oij] - k01C[oji];
+                    KcC[oji] = k10C[oij] - k10C[oji];
+                }
+            }
+            hsync();
+            // ---- observables: 13 trace jobs over the half's 8 warps (job = lw, lw + 8); then
+            // the energy (records, or the bf16 rows of the tensor-core forms) and <J^2>
+            for (int job = lw; job < kNTrace + 3; job += kHalfWarps) {
+                if (job == 0 || job == kNTrace + 1 || job == kNTrace + 2) {
+                    R v0 = A::rzero(), v1 = v0, v2 = v0, v3 = v0, v4 = v0, v5 = v0;
+                    if (job == 0) {
+                        for (int a = lane; a < n; a += 32) {
+                            const Z d = rhoC[cidx(a, a)];
+                            if (a < h) { v0 = A::radd(v0, d.x); v1 = A::radd(v1, d.y); }
+                            else { v2 = A::radd(v2, d.x); v3 = A::radd(v3, d.y); }
+                            const R jj = A::pick(p.obs.jj1, p.obs.jj1_d, a);
+                            v4 = A::rfma(jj, d.x, v4);
+                            v5 = A::rfma(jj, d.y, v5);
+                        }
+                    } else if (job == kNTrace + 1) {
+                        for (int a = lane; a < n; a += 32) {
+                            const R jpa = A::pick(p.obs.jp, p.obs.jp_d, a), jma = A::pick(p.obs.jm, p.obs.jm_d, a);
+                            const R mza = A::pick(p.obs.mz, p.obs.mz_d, a);
+                            if (A::nz(jpa)) {
+                                const Z r = rhoC[cidx(a + 1, a)];
+                                v0 = A::rfma(jpa, r.x, v0);
+                                v1 = A::rfma(jpa, r.y, v1);
+                            }
+                            if (A::nz(jma)) {
+                                const Z r = rhoC[cidx(a - 1, a)];
+                                v2 = A::rfma(jma, r.x, v2);
+                                v3 = A::rfma(jma, r.y, v3);
+                            }
+                            const Z d = rhoC[cidx(a, a)];
+                            v4 = A::rfma(mza, d.x, v4);
+                            v5 = A::rfma(mza, d.y, v5);
+                        }
+                    } else {
+                        for (int e = lane; e < p.obs.n_t1b; e += 32) {
+                            const int ix = p.obs.t1b_idx[e], r = ix >> 8, c = ix & 255;
+                            if ((r >= h) != (c >= h)) continue;
+                            const Z rv = rhoC[cidx(r, c)];
+                            const R tv = A::pick(p.obs.t1b_val, p.obs.t1b_val_d, e);
+                            v0 = A::rfma(tv, rv.x, v0);
+                            v1 = A::rfma(tv, rv.y, v1);
+                        }
+                    }
+                    const int s0 = job == 0 ? 0 : (job == kNTrace + 1 ? 10 : 4);
+                    const int cnt = job == kNTrace + 2 ? 2 : 6;
+                    const R vals[6] = {v0, v1, v2, v3, v4, v5};
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) {
+                        if (q >= cnt) break;
+                        const R v = A::wsum(vals[q]);
+                        const int slot = (job == 0 && q >= 4) ? 12 + q : s0 + q;
+                        if (lane == 0) fin2[slot] = A::dbl(v);
+                    }
+                } else if (p.iE2) {   // Q_{2mu} trace job - 1
+                    const int q = job - 1;
+                    R sr = A::rzero(), si = A::rzero();
+                    for (int e = p.obs.q_off[q] + lane; e < p.obs.q_off[q + 1]; e += 32) {
+                        const int ix = p.obs.q_idx[e], r = ix >> 8, c = ix & 255;
+                        if ((r >= h) != (c >= h)) continue;
+                        const Z rv = rhoC[cidx(r, c)];
+                        const R qv = A::pick(p.obs.q_val, p.obs.q_val_d, e);
+                        sr = A::rfma(qv, rv.x, sr);
+                        si = A::rfma(qv, rv.y, si);
+                    }
+                    sr = A::wsum(sr);
+                    si = A::wsum(si);
+                    if (lane == 0) {
+                        fin2[18 + 2 * q] = A::dbl(sr);
+                        fin2[19 + 2 * q] = A::dbl(si);
+                    }
+                }
+            }
+            auto put = [&](int slot, R v) {   // slot 0..3: energy re/im, <J^2> re/im
+                v = A::wsum(v);
+                if (lane == 0) pw2[slot * kHalfWarps + lw] = v;
+            };
+            if (p.tc_splits) {   // the gauge point's split-bf16 rows for the tensor-core contraction
+                const long long pt = pt0 + gi;
+                const int S = p.tc_splits, nk = p.tc_nk, npp = p.tc_nk - p.tc_nph;
+                for (int e = lt; e < nk; e += kHalfThreads) {
+                    const int src = p.tc_src[e];
+                    Z v = zero, y = zero;
+                    if (src >= 0) {
+                        const int r = src >> 8, c = src & 255;
+                        if ((r >= h) == (c >= h)) {   // the proton-neutron entries vanish
+                            if (e < p.tc_nph) {
+                                v = rhoC[cidx(r, c)];
+                            } else {
+                                v = KcC[cidx(c, r)];   // K10_rc, r < c
+                                y = KcC[cidx(r, c)];   // K01_rc
+                            }
+                        }
+                    }
+                    unsigned short tr[3], ti[3];
+                    bf16_terms(as_dd(v.x), S, tr);
+                    bf16_terms(as_dd(v.y), S, ti);
+                    for (int sp = 0; sp < S; ++sp) {
+                        p.tc_x[sp][(2 * pt) * nk + e] = tr[sp];
+                        p.tc_x[sp][(2 * pt + 1) * nk + e] = ti[sp];
+                    }
+                    if (e >= p.tc_nph) {
+                        bf16_terms(as_dd(y.x), S, tr);
+                        bf16_terms(as_dd(y.y), S, ti);
+                        const int ey = e - p.tc_nph;
+                        for (int sp = 0; sp < S; ++sp) {
+                            p.tc_y[sp][(2 * pt) * npp + ey] = tr[sp];
+                            p.tc_y[sp][(2 * pt + 1) * npp + ey] = ti[sp];
+                        }
+                    }
+                }
+                if (lane == 0) {
+                    pw2[lw] = A::rzero();
+                    pw2[kHalfWarps + lw] = A::rzero();
+                }
+            } else {   // two-body energy: the point kernel's record loop on the compact blocks
+                const R quarter = A::rconst(0.25f);
+                Z e2 = zero;
+                // same-species records: all four indices in species block b
+                for (int e = lt; e < p.nrec_gen; e += kHalfThreads) {
+                    const uint32_t pk = p.rec_idx[e];
+                    const R v = A::pick(p.rec_v, p.rec_vd, e);
+                    int i = pk & 0xff, j = (pk >> 8) & 0xff, k = (pk >> 16) & 0xff, l = pk >> 24;
+                    const bool sym = i + j != k + l;
+                    const int b = i >= h ? 1 : 0, o = b * bs;
+                    i -= b * h;
+                    j -= b * h;
+                    k -= b * h;
+                    l -= b * h;
+                    Z t = rhoC[o + k * hl + i] * rhoC[o + l * hl + j];
+                    t = zfms(rhoC[o + l * hl + i], rhoC[o + k * hl + j], t);
+                    Z u = KcC[o + i * hl + j] * KcC[o + l * hl + k];
+                    if (sym) {
+                        t = zfma(rhoC[o + i * hl + k], rhoC[o + j * hl + l], t);
+                        t = zfms(rhoC[o + j * hl + k], rhoC[o + i * hl + l], t);
+                        u = zfma(KcC[o + k * hl + l], KcC[o + j * hl + i], u);
+                    }
+                    t = rfma(quarter, u, t);
+                    e2 = rfma(v, t, e2);
+                }
+                // proton-neutron records: (i, k) protons, (j, l) neutrons; only the direct terms
+                for (int e = p.nrec_gen + lt; e < p.nrec; e += kHalfThreads) {
+                    const uint32_t pk = p.rec_idx[e];
+                    const R v = A::pick(p.rec_v, p.rec_vd, e);
+                    const int i = pk & 0xff, j = ((pk >> 8) & 0xff) - h, k = (pk >> 16) & 0xff, l = (pk >> 24) - h;
+                    Z t = rhoC[k * hl + i] * rhoC[bs + l * hl + j];
+                    if (i + j != k + l) t = zfma(rhoC[i * hl + k], rhoC[bs + j * hl + l], t);
+                    e2 = rfma(v, t, e2);
+                }
+                put(0, e2.x);
+                put(1, e2.y);
+            }
+            {   // <J^2>, the same terms as the single-point path, within the species blocks
+                const R half_ = A::rconst(0.5f);
+                Z rest = zero;
+                for (int t = lt; t < 2 * hh; t += kHalfThreads) {
+                    const int blk = t >= hh ? 1 : 0, e = t - blk * hh;
+                    const int a = blk * h + e / h, c = blk * h + e % h;
+                    const R jpa = A::pick(p.obs.jp, p.obs.jp_d, a), jma = A::pick(p.obs.jm, p.obs.jm_d, a);
+                    const R jpc = A::pick(p.obs.jp, p.obs.jp_d, c), jmc = A::pick(p.obs.jm, p.obs.jm_d, c);
+                    const R mzz = A::rmul(A::pick(p.obs.mz, p.obs.mz_d, a), A::pick(p.obs.mz, p.obs.mz_d, c));
+                    const int ac = cidx(a, c);
+                    Z q = mzz * (k10C[ac] * k01C[ac]);
+                    q = zfms(mzz * rhoC[ac], rhoC[cidx(c, a)], q);
+                    if (A::nz(jpa) && A::nz(jmc))
+                        q = zfms(A::rmul(jpa, jmc) * rhoC[ac + hl], rhoC[cidx(c - 1, a)], q);
+                    if (A::nz(jpa) && A::nz(jpc))
+                        q = zfma(A::rmul(half_, A::rmul(jpa, jpc)) * k10C[ac + hl], k01C[ac + 1], q);
+                    if (A::nz(jma) && A::nz(jmc))
+                        q = zfma(A::rmul(half_, A::rmul(jma, jmc)) * k10C[ac - hl], k01C[ac - 1], q);
+                    rest = rest + q;
+                }
+                put(2, rest.x);
+                put(3, rest.y);
+            }
+        }
+        hsync();
+        if (lw == 0) {   // accumulation over this half's gauge points (single-lane FP64 values)
+            const unsigned full = 0xffffffffu;
+            R ws[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) ws[q] = A::wsum(lane < kHalfWarps ? pw2[q * kHalfWarps + lane] : A::rzero());
+            const bool eval = !p.norm_only && !sing;
+            zc norm = mk(0.0, 0.0);
+            if (lane == 0) {
+                const zc zph = mk(p.gphase[2 * gi], p.gphase[2 * gi + 1]);
+                norm = (p.vacfac * det0 * det1) * (pf * zph);
+            }
+            norm.x = __shfl_sync(full, norm.x, 0);
+            norm.y = __shfl_sync(full, norm.y, 0);
+            zc o = mk(0.0, 0.0), hg = mk(0.0, 0.0);
+            bool use = eval;
+            if ((lane == 6 || (lane == 0 && gout)) && eval)
+                hg = mk(fin2[4] + A::dbl(ws[0]) + p.e0, fin2[5] + A::dbl(ws[1]));
+            if (lane == 1) o = mk(fin2[0], fin2[1]);
+            else if (lane == 2) o = mk(fin2[2], fin2[3]);
+            else if (lane == 3) o = mk(fin2[4], fin2[5]);
+            else if (lane == 6) o = hg;
+            else if (lane == 7) {
+                const zc trp = mk(fin2[10], fin2[11]), trm = mk(fin2[12], fin2[13]), trz = mk(fin2[14], fin2[15]);
+                o = mk(fin2[16] + A::dbl(ws[2]), fin2[17] + A::dbl(ws[3])) + trp * trm + trz * trz;
+            } else if (lane >= 8 && lane < 18 && p.iE2) o = mk(fin2[2 * lane + 2], fin2[2 * lane + 3]);
+            else use = false;
+            if (p.tc_splits && lane == 0) {
+                const long long pt = pt0 + gi;
+                const double inv = 1.0 / ((double)p.nfom * p.nfom);
+                p.tc_w[2 * pt] = eval ? inv * norm.x : 0.0;
+                p.tc_w[2 * pt + 1] = eval ? inv * norm.y : 0.0;
+            }
+            if (lane == 0) {
+                acc2[0] = acc2[0] + norm;
+                if (gout) {
+                    double *g = gout + 4LL * (((long long)pair * p.n_euler + ie) * p.n_gauge + gi);
+                    g[0] = norm.x;
+                    g[1] = norm.y;
+                    g[2] = hg.x;
+                    g[3] = hg.y;
+                }
+                int f = (under == 1) ? 1 : (under == 2 ? 4 : 0);
+                if (!p.norm_only && sing) f |= 2;
+                sh2[8] |= f;
+            }
+            if (use) acc2[lane] = zfma(norm, o, acc2[lane]);
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {   // the two halves' sums
+        const zc *a0 = reinterpret_cast<const zc *>(smem + p.place.off_half + L.acc);
+        const zc *a1 = reinterpret_cast<const zc *>(smem + p.place.off_half + L.bytes + L.acc);
+        const int f0 = reinterpret_cast<const int *>(smem + p.place.off_half + L.sh)[8];
+        const int f1 = reinterpret_cast<const int *>(smem + p.place.off_half + L.bytes + L.sh)[8];
+        const double inv = 1.0 / ((double)p.nfom * p.nfom);
+        int f = f0 | f1;
+        for (int io = 0; io < kNobs; ++io) {
+            const zc v = io == kNobs - 1 ? mk(0.0, 0.0) : inv * (a0[io] + a1[io]);
+            if (!zfinite(v)) f |= 4;
+            zout[2LL * (io * p.n_euler + ie)] = v.x;
+            zout[2LL * (io * p.n_euler + ie) + 1] = v.y;
+        }
+        status[(long long)pair * p.n_euler + ie] = f;
+    }
+    __syncthreads();
+}
+
 // One work item: Euler point `ie` of pair `pair`, all its gauge points, in the
 // CTA's workspace `slot`. `reload` is set when the previous item of this CTA
 // belonged to another pair (or context): V0^T, U0^T and the phase tables are
@@ -960,6 +1407,8 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
         // the solve and the densities are block-diagonal; both species are eliminated together
         // on compact h x h blocks
         const bool split = reduced && pr[p.pl.dets + 6] != 0.0;
+        // two gauge points in flight (split_pair_points) when the halves' storage fits
+        const bool use2 = pl.sp2 && split && p.nfom > 1 && !r2out && !r1out && blockDim.x == kThreads;
         double *zout = zres + 2LL * (long long)pair * kNobs * p.n_euler;
         if (pst) {
             for (int io = threadIdx.x; io < kNobs; io += blockDim.x) {
@@ -977,9 +1426,19 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
             __syncthreads();
             for (int t = threadIdx.x; t < nn; t += blockDim.x) {
                 const int k = t / n, j = t % n;
-                V0t[t] = A::real(gV0[j * n + k]);
-                U0t[t] = A::real(gU0[j * n + k]);
+                if (!use2) {
+                    V0t[t] = A::real(gV0[j * n + k]);
+                    U0t[t] = A::real(gU0[j * n + k]);
+                }
                 CZ[t] = A::from(mk(-p.cscale * (reduced ? gZi[t] : gZ0[t]), 0.0));
+            }
+            if (use2) {   // the diagonal species blocks only: [b][k][j] = V0(b h + j, b h + k)
+                R *V0c = reinterpret_cast<R *>(smem + pl.off_uvc), *U0c = V0c + 2 * h * h;
+                for (int t = threadIdx.x; t < 2 * h * h; t += blockDim.x) {
+                    const int b = t / (h * h), e = t % (h * h), k = e / h, j = e % h;
+                    V0c[t] = A::real(gV0[(b * h + j) * n + b * h + k]);
+                    U0c[t] = A::real(gU0[(b * h + j) * n + b * h + k]);
+                }
             }
             for (int l = threadIdx.x; l < p.nfom; l += blockDim.x) {
                 const zc e = expi(p.nfom == 1 ? 0.0 : twopi * l / p.nfom);
@@ -1057,6 +1516,10 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
             B[t] = A::from(v);
         }
         __syncthreads();
+        if (use2) {
+            split_pair_points<Z>(p, smem, X, P, B, CZ, ephz, pfz, det0, det1, pair, ie, pt0, gout, zout, status);
+            return;
+        }
 
         int flags = 0;
         const Z zero = A::from(mk(0.0, 0.0));
@@ -1442,7 +1905,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     // PNAMP_Energy_OpenMP.f90:40-78:
                     // V[rho_ki rho_lj - rho_li rho_kj + d(rho_ik rho_jl - rho_jk rho_il)]
                     // + V/4 [K01_ij K10_kl + d K01_kl K10_ij],  K_xy = kappa_xy - kappa_yx
-                    const R quarter = A::real(0.25);
+                    const R quarter = A::rconst(0.25f);
                     Z e2 = zero;
                     auto rec = [&](uint32_t pk, R v) {
                         const int i = pk & 0xff, j = (pk >> 8) & 0xff, k = (pk >> 16) & 0xff, l = pk >> 24;
@@ -1473,7 +1936,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         const R v0 = A::pick(p.rec_v, p.rec_vd, e);
                         const bool two = e1 < ngen;
                         const uint32_t pk1 = two ? p.rec_idx[e1] : 0u;
-                        const R v1 = two ? A::pick(p.rec_v, p.rec_vd, e1) : A::real(0.0);
+                        const R v1 = two ? A::pick(p.rec_v, p.rec_vd, e1) : A::rzero();
                         rec(pk0, v0);
                         if (two) rec(pk1, v1);
                     }
@@ -1483,7 +1946,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                         const R v0 = A::pick(p.rec_v, p.rec_vd, e);
                         const bool two = e1 < p.nrec;
                         const uint32_t pk1 = two ? p.rec_idx[e1] : 0u;
-                        const R v1 = two ? A::pick(p.rec_v, p.rec_vd, e1) : A::real(0.0);
+                        const R v1 = two ? A::pick(p.rec_v, p.rec_vd, e1) : A::rzero();
                         rec_pn(pk0, v0);
                         if (two) rec_pn(pk1, v1);
                     }
@@ -1494,15 +1957,15 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                     // Jx, Jy = (J+ +- J-)/(2, 2i):  sum_a j(j+1) rho_aa [above]
                     // + Tr(J+ rho) Tr(J- rho) + Tr(Jz rho)^2 - Tr(J+ rho J- rho) - Tr(Jz rho Jz rho)
                     // + [Tr(J+ k10 J+ k01^T) + Tr(J- k10 J- k01^T)]/2 + Tr(Jz k10 Jz k01^T)
-                    const R half = A::real(0.5);
+                    const R half = A::rconst(0.5f);
                     Z rest = zero;
-                    const int dq = blockDim.x / n, dr = blockDim.x % n;
-                    int a = threadIdx.x / n, c = threadIdx.x % n;
-                    for (int t = threadIdx.x; t < nn; t += blockDim.x, a += dq, c += dr) {
-                        if (c >= n) {
-                            c -= n;
-                            ++a;
-                        }
+                    // a species-split pair has no proton-neutron densities and J+-, Jz keep the
+                    // species, so every term with a and c of different species vanishes: only the
+                    // two diagonal h x h blocks are summed (index t -> block, row, column)
+                    const int cnt = split ? 2 * h * h : nn, w = split ? h : n;
+                    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+                        const int blk = split ? t / (h * h) : 0, e = t - blk * h * h;
+                        const int a = blk * h + e / w, c = blk * h + e % w;
                         const R jpa = A::pick(p.obs.jp, p.obs.jp_d, a), jma = A::pick(p.obs.jm, p.obs.jm_d, a);
                         const R jpc = A::pick(p.obs.jp, p.obs.jp_d, c), jmc = A::pick(p.obs.jm, p.obs.jm_d, c);
                         const R mzz = A::rmul(A::pick(p.obs.mz, p.obs.mz_d, a), A::pick(p.obs.mz, p.obs.mz_d, c));

@@ -7,13 +7,78 @@ N^-1/2 H N^-1/2 in that subspace. `gcm_levels` assembles, for each even J, the
 basis (q, K), K = -J..J, from the projected N^J_{K1K2}(q, q') and
 H^J_{K1K2}(q, q') of every computed pair (q <= q'; the other triangle by
 Hermiticity, N^J_{K1K2}(q', q) = conj(N^J_{K2K1}(q, q'))) and returns the levels.
-Host-side: a few matrices of size (number of vacua x (2J+1)).
+Host-side by default: a few matrices of size (number of vacua x (2J+1)).
+`hndiag_batch_gpu` solves a batch of such problems on the GPU, one CTA each
+(`include/pnamp_gcm.h`, `sccm_gb300/csrc/hw_kernels.cu`); `gcm_levels(..., gpu=True)`
+puts every angular momentum and every vacuum's K-mixing of a basis in one launch.
 """
 from __future__ import annotations
 
 import numpy as np
 
 from .basis import JJMAX
+
+
+HW_EXPORTS = ("pnamp_hw_work_bytes", "pnamp_hw_solve")
+
+
+def _hw_lib():
+    import ctypes as C
+    from .pnamp import load_library
+    lib = load_library()
+    if not getattr(lib, "_hw_bound", False):
+        vp = C.c_void_p
+        lib.pnamp_hw_work_bytes.restype = C.c_longlong
+        lib.pnamp_hw_work_bytes.argtypes = [C.c_int, vp]
+        lib.pnamp_hw_solve.argtypes = [C.c_int, vp, vp, vp, vp, C.c_double, vp, vp, vp, vp, vp]
+        lib._hw_bound = True
+    return lib
+
+
+def hndiag_batch_gpu(problems, eps=1e-5, vectors=False, device="cuda"):
+    """HNDIAG for a batch of (H, N) pairs on the GPU, one CTA per problem.
+
+    Returns per problem (E ascending over the kept subspace, number kept, F): F (only with
+    `vectors`) holds the solutions f_k in its columns, normalised f_k^+ N f_k = 1."""
+    import ctypes as C
+    import torch
+    lib = _hw_lib()
+    dims = np.array([np.asarray(H).shape[0] for H, _ in problems], dtype=np.int32)
+    offs = np.zeros(len(problems), dtype=np.int64)
+    if len(problems) > 1:
+        offs[1:] = np.cumsum(dims.astype(np.int64) ** 2)[:-1]
+    tot = int((dims.astype(np.int64) ** 2).sum())
+    Hh = np.concatenate([np.ascontiguousarray(H, dtype=np.complex128).ravel() for H, _ in problems]) if tot else \
+        np.zeros(1, np.complex128)
+    Nh = np.concatenate([np.ascontiguousarray(N, dtype=np.complex128).ravel() for _, N in problems]) if tot else \
+        np.zeros(1, np.complex128)
+    dev = torch.device(device)
+    Hd = torch.from_numpy(Hh.view(np.float64)).to(dev)
+    Nd = torch.from_numpy(Nh.view(np.float64)).to(dev)
+    E = torch.zeros(max(tot, 1), dtype=torch.float64, device=dev)
+    kept = torch.zeros(max(len(problems), 1), dtype=torch.int32, device=dev)
+    F = torch.zeros(2 * max(tot, 1), dtype=torch.float64, device=dev) if vectors else None
+    nb = lib.pnamp_hw_work_bytes(len(problems), dims.ctypes.data)
+    if nb < 0:
+        raise ValueError("problem sizes out of range")
+    work = torch.empty(max(nb, 1), dtype=torch.uint8, device=dev)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    # E takes problem b's energies at off[b] (a slot of dim[b]^2 doubles, the first dim[b] used)
+    rc = lib.pnamp_hw_solve(len(problems), dims.ctypes.data, offs.ctypes.data, C.c_void_p(Hd.data_ptr()),
+                            C.c_void_p(Nd.data_ptr()), float(eps), C.c_void_p(E.data_ptr()),
+                            C.c_void_p(kept.data_ptr()), C.c_void_p(F.data_ptr()) if vectors else None,
+                            C.c_void_p(work.data_ptr()), C.c_void_p(st))
+    if rc != 0:
+        raise RuntimeError(f"pnamp_hw_solve failed with code {rc}")
+    torch.cuda.synchronize(dev)
+    Eh, kh = E.cpu().numpy(), kept.cpu().numpy()
+    Fh = F.cpu().numpy().view(np.complex128) if vectors else None
+    out = []
+    for b, (m, o) in enumerate(zip(dims, offs)):
+        k = int(kh[b])
+        f = Fh[o:o + m * m].reshape(m, m)[:, :k].copy() if vectors else None
+        out.append((Eh[o:o + k].copy(), k, f))
+    return out
 
 
 def hndiag(H, N, eps=1e-5, nos=None):
@@ -110,13 +175,16 @@ def assemble(kernels, pairs, nvac, J, field):
     return M
 
 
-def gcm_levels(kernels, pairs, nvac, jvals=(0, 2, 4, 6), eps=1e-5, axial=False):
+def gcm_levels(kernels, pairs, nvac, jvals=(0, 2, 4, 6), eps=1e-5, axial=False, gpu=False):
     """Lowest GCM energies per J and the K-mixed projected energy of each vacuum.
 
     `kernels[k]` holds the projected fields of pair `pairs[k]` (njkk, hjkk arrays
-    [J][K1+6][K2+6]); `axial` restricts the basis to K = 0.
+    [J][K1+6][K2+6]); `axial` restricts the basis to K = 0; `gpu` solves every problem
+    in one batched launch (`hndiag_batch_gpu`) instead of numpy.
     Returns {J: {"levels": array, "per_q": array(nvac)}}.
     """
+    if gpu:
+        return _gcm_levels_gpu(kernels, pairs, nvac, jvals, eps, axial)
     out = {}
     for J in jvals:
         if axial:
@@ -140,6 +208,41 @@ def gcm_levels(kernels, pairs, nvac, jvals=(0, 2, 4, 6), eps=1e-5, axial=False):
             if mq:
                 per_q[q] = e[0]
         out[J] = {"levels": levels, "per_q": per_q, "kept": m}
+    return out
+
+
+def _basis_matrices(kernels, pairs, nvac, J, axial):
+    d = 1 if axial else 2 * J + 1
+    sl = slice(JJMAX, JJMAX + 1) if axial else slice(JJMAX - J, JJMAX + J + 1)
+    Nm = np.zeros((nvac * d, nvac * d), complex)
+    Hm = np.zeros_like(Nm)
+    for (i, j), k in zip(pairs, kernels):
+        for M, f in ((Nm, "njkk"), (Hm, "hjkk")):
+            blk = k[f][J, sl, sl]
+            M[i * d:(i + 1) * d, j * d:(j + 1) * d] = blk
+            if i != j:
+                M[j * d:(j + 1) * d, i * d:(i + 1) * d] = blk.conj().T
+    return Hm, Nm, d
+
+
+def _gcm_levels_gpu(kernels, pairs, nvac, jvals, eps, axial):
+    probs, index = [], []
+    for J in jvals:
+        Hm, Nm, d = _basis_matrices(kernels, pairs, nvac, J, axial)
+        probs.append((Hm, Nm))
+        index.append((J, None))
+        for q in range(nvac):
+            s = slice(q * d, (q + 1) * d)
+            probs.append((Hm[s, s], Nm[s, s]))
+            index.append((J, q))
+    res = hndiag_batch_gpu(probs, eps)
+    out = {J: {"levels": None, "per_q": np.full(nvac, np.nan), "kept": 0} for J in jvals}
+    for (J, q), (e, k, _) in zip(index, res):
+        if q is None:
+            out[J]["levels"] = e
+            out[J]["kept"] = k
+        elif k:
+            out[J]["per_q"][q] = e[0]
     return out
 
 

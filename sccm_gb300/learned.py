@@ -453,8 +453,56 @@ class LearnedPNAMP:
         self.last_timing = tm
         return res
 
-    def run_gcm(self, pairs, nvac, jvals=(0, 2, 4, 6), eps=1e-5, nlev=3, exact_ctx=None):
+    def coarse_kernels(self, pairs):
+        """Projected N^J, H^J of `pairs` from the exact coarse-mesh kernels alone (cheap: the
+        coarse mesh has P_coarse / P_fine of the points), as per-pair dicts."""
+        out = []
+        for s in range(0, len(pairs), self.cfg.chunk):
+            chunk = pairs[s:s + self.cfg.chunk]
+            npairs = len(chunk)
+            uv, _ = self._upload(chunk)
+            z = torch.zeros((npairs, NOBS, self.Pc, 2), dtype=torch.float64, device=self.dev)
+            st = torch.zeros((npairs, self.Pc), dtype=torch.int32, device=self.dev)
+            self.coarse.batch_device(npairs, uv.data_ptr(), z.data_ptr(), st.data_ptr(), self._stream())
+            o = torch.zeros((npairs, FIELDS, JJMAX + 1, NK, NK, 2), dtype=torch.float64, device=self.dev)
+            self.coarse.project_device(npairs, z.data_ptr(), o.data_ptr(), False, self._stream())
+            c = o.cpu().numpy()
+            c = c[..., 0] + 1j * c[..., 1]
+            out += [{"pair": tuple(chunk[k]), "njkk": c[k, 0], "hjkk": c[k, 1]} for k in range(npairs)]
+        return out
+
+    def precheck(self, pairs, nvac, jvals=(0, 2, 4, 6), eps=1e-5, nlev=3):
+        """Bound on the GCM-level error the learned kernels could reach, before any fine-mesh work.
+
+        The Hill-Wheeler weights come from the coarse-mesh kernels; each pair's H^J error is
+        taken at the level the flagging aims for (flag_kev in the basis of normalised states,
+        times sqrt(N^J(q,q) N^J(q',q')) from the coarse diagonal norms), so the bound is what
+        the mode achieves at best. Returns (bound in keV, coarse kernels)."""
+        from .gcm import level_weights
+        ck = self.coarse_kernels(pairs)
+        W = level_weights(ck, pairs, nvac, jvals, eps, nlev)
+        diag = {}
+        for r in ck:
+            i, j = r["pair"]
+            if i == j:
+                diag[i] = {J: float(np.abs(np.diagonal(r["njkk"][J])).max()) for J in jvals}
+        bound = 0.0
+        for J in jvals:
+            tot = 0.0
+            for p, (i, j) in enumerate(pairs):
+                if i in diag and j in diag:
+                    sc = math.sqrt(diag[i][J] * diag[j][J])
+                    tot += W[J][p] * (2 * J + 1) * self.cfg.flag_kev * 1e-3 * sc
+            bound = max(bound, tot)
+        return bound * 1e3, ck
+
+    def run_gcm(self, pairs, nvac, jvals=(0, 2, 4, 6), eps=1e-5, nlev=3, exact_ctx=None, train_pairs=None):
         """`run` over the complete pair set of `nvac` vacua, then the Hill-Wheeler gate.
+
+        First `precheck`: when even the flagging's target error would leave more than
+        gcm_kev on the GCM levels, every pair goes to the full mesh at once (no training, no
+        norm pass, no network), so the mode costs the exact quadrature plus the coarse pass.
+        Otherwise the network is trained on `train_pairs` (if given) and the mode runs.
 
         Each pair's estimated H^J block error is (2J+1)^2 x its held-out estimate (the
         spectral norm of a (2J+1)^2 block whose entries are each at most (2J+1) x the
@@ -467,6 +515,17 @@ class LearnedPNAMP:
         cfg = self.cfg
         torch.cuda.synchronize()
         t0 = time.perf_counter()
+        pre, _ = self.precheck(pairs, nvac, jvals, eps, nlev)
+        if pre > cfg.gcm_kev:
+            res = [dict(r, fallback=True, gated=True, exact_euler=self.P, est_err_MeV=0.0)
+                   for r in self.exact(pairs, ctx=exact_ctx)]
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            self.last_timing = {"precheck_then_exact": t1 - t0}
+            return res, {"precheck_bound_keV": pre, "bound_before_keV": None, "bound_after_keV": 0.0,
+                         "gated_pairs": len(pairs), "fallback_pairs": 0, "run_s": t1 - t0, "gate_s": 0.0,
+                         "exact_fraction": 1.0, "decision": "all pairs exact: the precheck bound exceeds gcm_kev"}
+        train_rec = self.train(train_pairs) if train_pairs else None
         res = self.run(pairs)
         t1 = time.perf_counter()
         W = level_weights(res, pairs, nvac, jvals, eps, nlev)
@@ -493,9 +552,10 @@ class LearnedPNAMP:
                 res[p]["exact_euler"] = self.P
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        rec = {"bound_before_keV": b0, "bound_after_keV": bound(), "gated_pairs": len(gated),
+        rec = {"precheck_bound_keV": pre, "bound_before_keV": b0, "bound_after_keV": bound(),
+               "gated_pairs": len(gated), "decision": "learned, with the gate",
                "fallback_pairs": int(sum(r["fallback"] for r in res if not r.get("gated"))),
-               "run_s": t1 - t0, "gate_s": t2 - t1,
+               "run_s": t1 - t0, "gate_s": t2 - t1, "training": train_rec,
                "exact_fraction": float(sum(r["exact_euler"] for r in res)) / (self.P * len(res))}
         return res, rec
 

@@ -32,9 +32,10 @@ def test_library_exports_declared_symbols(lib):
 
 
 def test_python_host_binds_every_export():
+    from sccm_gb300.gcm import HW_EXPORTS
     from sccm_gb300.mlp import MLP_EXPORTS
     from sccm_gb300.pnamp import EXPORTS
-    assert sorted(EXPORTS + MLP_EXPORTS) == declared_symbols()
+    assert sorted(EXPORTS + MLP_EXPORTS + HW_EXPORTS) == declared_symbols()
 
 
 def test_strerror_and_version(lib):

@@ -47,6 +47,22 @@ def test_norm_exact_and_energy_kernel_within_1kev(trained):
     assert err["max_kernel_EJ_err_keV"] <= 1.0
 
 
+def test_hill_wheeler_gate_meets_the_level_gates(trained):
+    """run_gcm over the complete pair set: the coarse precheck, the learned run and the gate
+    leave the lowest GCM levels and every vacuum's E_J within gcm_kev (1 keV) of the full
+    quadrature, whichever way the precheck decides."""
+    wl, lm, _ = trained
+    nvac = len(wl.vacua)
+    res, rec = lm.run_gcm(wl.pairs, nvac)
+    exact = lm.exact(wl.pairs)
+    err = energy_errors_kev(res, exact, nvac=nvac, pairs=wl.pairs)
+    print(rec["decision"], rec["precheck_bound_keV"], err["gcm_levels_err_keV"], err["EJ_per_vacuum_err_keV"])
+    assert err["gcm_levels_err_keV"] <= lm.cfg.gcm_kev
+    assert err["EJ_per_vacuum_err_keV"] <= lm.cfg.gcm_kev
+    for a, b in zip(res, exact):
+        assert np.abs(a["njkk"] - b["njkk"]).max() <= 1e-12 * np.abs(b["njkk"]).max()
+
+
 def test_network_gains_over_interpolation_alone(trained):
     wl, lm, _ = trained
     rms_interp, rms_net = lm.validation_rms(wl.pairs[:10], n_euler=32)   # fresh Euler points

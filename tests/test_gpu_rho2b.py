@@ -46,7 +46,9 @@ def test_rho2b_matches_oracle(case, form):
         z, st, r2 = ctx.batch_rho2b([(*w.vacua[i], *w.vacua[j]) for i, j in pairs])
         vals = [ctx.project_rho2b(z[k], r2[k]) for k in range(len(pairs))]
         z_plain, st_plain = ctx.batch([(*w.vacua[i], *w.vacua[j]) for i, j in pairs])
-    assert np.array_equal(z, z_plain) and np.array_equal(st, st_plain)   # observables untouched
+    # observables untouched: the plain launch runs split pairs two gauge points at a time and
+    # adds the two halves' sums at the end, so the values agree to rounding, not bit for bit
+    assert np.abs(z - z_plain).max() <= 1e-13 * np.abs(z_plain).max() and np.array_equal(st, st_plain)
     wts = w.mesh.euler_points()[:, 3]
     terms = [list(zip(tab["term_q"][a:b], tab["term_c"][a:b])) for a, b in zip(tab["ptr"][:-1], tab["ptr"][1:])]
     for k, (i, j) in enumerate(pairs):

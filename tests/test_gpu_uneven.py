@@ -20,7 +20,10 @@ pytestmark = pytest.mark.gpu
 
 NORM_TOL = 1e-10
 OBS_TOL = 1e-9
-SAME_TOL = 1e-13   # multi-context vs single-context launch of the same point code
+# multi-context vs single-context launch: the same point code, except that a context whose
+# shared-memory budget cannot hold two gauge points runs species-split pairs one point at a
+# time, which sums the gauge points in another order (double-float rounding, ~3e-13)
+SAME_TOL = 1e-12
 
 
 def _workloads():
