@@ -1547,7 +1547,7 @@ __device__ __forceinline__ void point_item(const Params &p, const double *__rest
                 zc pf = mk(0.0, 0.0);
                 bool sing = false;
                 if (concg) {
-                    constexpr int kPfWarpsG = 4;
+                    constexpr int kPfWarpsG = 3;
                     if (wid < kPfWarpsG) {
                         const Grp g{(int)threadIdx.x, kPfWarpsG * 32, wid, 1};
                         for (int t = g.tid; t < n * (n - 1) / 2; t += g.nthr) {

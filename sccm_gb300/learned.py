@@ -516,14 +516,17 @@ class LearnedPNAMP:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         pre, _ = self.precheck(pairs, nvac, jvals, eps, nlev)
+        torch.cuda.synchronize()
+        tp = time.perf_counter()
         if pre > cfg.gcm_kev:
             res = [dict(r, fallback=True, gated=True, exact_euler=self.P, est_err_MeV=0.0)
                    for r in self.exact(pairs, ctx=exact_ctx)]
             torch.cuda.synchronize()
             t1 = time.perf_counter()
-            self.last_timing = {"precheck_then_exact": t1 - t0}
+            self.last_timing = {"precheck": tp - t0, "exact": t1 - tp}
             return res, {"precheck_bound_keV": pre, "bound_before_keV": None, "bound_after_keV": 0.0,
                          "gated_pairs": len(pairs), "fallback_pairs": 0, "run_s": t1 - t0, "gate_s": 0.0,
+                         "precheck_s": tp - t0, "exact_s": t1 - tp, "training": None,
                          "exact_fraction": 1.0, "decision": "all pairs exact: the precheck bound exceeds gcm_kev"}
         train_rec = self.train(train_pairs) if train_pairs else None
         res = self.run(pairs)
