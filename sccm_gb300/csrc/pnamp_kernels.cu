@@ -740,7 +740,9 @@ __device__ zc pfaffian_upper_g(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fl
             pv[2 + b] = f ? ssz : zrecip(ssz);
         }
     };
-    if (nstep > 0 && wid < NB) search(wid, 0);
+    // warp w serves matrices w, w + nwg, ...: one warp per matrix, or one warp for both
+    const int nwg = g.nthr >> 5;
+    for (int b = wid; nstep > 0 && b < NB; b += nwg) search(b, 0);
     gsync(g);
     for (int k = 0; k < nstep; ++k) {
         const int r = 2 * k, c = r + 1;
@@ -786,9 +788,9 @@ __device__ zc pfaffian_upper_g(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fl
         gsync(g);
         // (b) S_ij += v_i S_rj - S_ri v_j for c < i < j; row c + 1 (the next pivot row) first
         const bool more = k + 1 < nstep;
-        if (wid < NB) {
-            Z *Sb = S + wid * hh;
-            const Z *vb = vec + wid * h;
+        for (int b = wid; b < NB; b += nwg) {
+            Z *Sb = S + b * hh;
+            const Z *vb = vec + b * h;
             const int i = c + 1;
             const Z vi = vb[i], sri = Sb[r * h + i];
             for (int j = i + 1 + lane; j < h; j += 32) {
@@ -798,7 +800,7 @@ __device__ zc pfaffian_upper_g(const Grp &g, Z *S, int h, Z *vec, Z *pv, int *fl
                 Sb[i * h + j] = sv;
             }
             __syncwarp();
-            if (more) search(wid, c + 1);
+            if (more) search(b, c + 1);
         }
         const int mm = h - c - 2, TT = mm * (mm - 1) / 2;
         for (int t = g.tid; t < NB * TT; t += g.nthr) {
@@ -1015,6 +1017,9 @@ __device__ __forceinline__ void split_pair_points(const Params &p, unsigned char
     // compact V0^T, U0^T: species b, [b][k][j] = V0(b h + j, b h + k)
     const R *V0c = reinterpret_cast<const R *>(smem + p.place.off_uvc), *U0c = V0c + 2 * hh;
     const int barH = 3 + 3 * half;
+    // one warp eliminates both species' Pfaffians (it finished at half the solve's time on
+    // two), so the Gauss-Jordan group, the critical path, has seven of the half's eight warps
+    constexpr int kPfW2 = 1;
     auto hsync = [&]() { asm volatile("bar.sync %0, %1;" ::"r"(barH), "r"(kHalfThreads) : "memory"); };
     // compact index of (r, c), r and c of the same species
     auto cidx = [&](int r, int c) {
@@ -1033,8 +1038,8 @@ __device__ __forceinline__ void split_pair_points(const Params &p, unsigned char
         int under = 0;
         zc pf = mk(0.0, 0.0);
         bool sing = false;
-        if (lw < 2) {   // the two species' Schur-complement blocks and their Pfaffians
-            const Grp g{lt, 64, lw, 1 + 3 * half};
+        if (lw < kPfW2) {   // the two species' Schur-complement blocks and their Pfaffians
+            const Grp g{lt, 32 * kPfW2, lw, 1 + 3 * half};
             const int Th = h * (h - 1) / 2;
             for (int t = g.tid; t < 2 * Th; t += g.nthr) {
                 const int b = t >= Th ? 1 : 0;
@@ -1047,7 +1052,7 @@ __device__ __forceinline__ void split_pair_points(const Params &p, unsigned char
             pf = pfaffian_upper_g<Z, 2>(g, S2, h, vec2, pfs2, sh2, under);
             pf = pf * pfz;   // meaningful in the half's thread 0
         } else if (!p.norm_only) {   // T22 blocks, right-hand sides, Y T22^-1
-            const Grp g{lt - 64, kHalfThreads - 64, lw - 2, 2 + 3 * half};
+            const Grp g{lt - 32 * kPfW2, kHalfThreads - 32 * kPfW2, lw - kPfW2, 2 + 3 * half};
             for (int t = g.tid; t < 2 * hh; t += g.nthr) {
                 const int b = t >= hh ? 1 : 0, e = t - b * hh, i = e / h, j = e % h;
                 const int gg = (b * h + i) * n + b * h + j;
