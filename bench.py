@@ -286,7 +286,7 @@ def learned_main(args):
     timing = dict(lm.last_timing)
     if gate["decision"].startswith("all pairs exact"):
         # the mode ran the plain quadrature itself after its precheck: that part is the exact
-        # mixed form's time, and its kernels are the judge
+        # mixed form's time, and its kernels are the reference values
         exact, te = learned, gate["exact_s"]
     else:
         exact, te = timed(lambda: lm.exact(wl.pairs))

@@ -97,9 +97,9 @@ def test_ti48_kb3g_pairs_on_triaxial_mesh_match_oracle(ti48, form):
 def test_ti48_ill_conditioned_kets_match_high_precision(ti48, form):
     """Kets with cond(U1) ~ 1e4-1e5 (vacua 0 and 1): the reference's sequence, which inverts
     the rotated U1 at every point (PNAMP_Proj.f90:162-184), loses up to ~1e-8 of the gauge-
-    summed norm there, so the FP64 restatement cannot judge at 1e-10. The judge is the same
-    formula in 30-digit arithmetic (tests/golden/make_ti48_highprec.py) at the Euler points
-    where the FP64 sequence is worst; the GPU must be within 1e-10 of it."""
+    summed norm there, so the FP64 restatement cannot decide at 1e-10. The reference value
+    is the same formula in 30-digit arithmetic (tests/golden/make_ti48_highprec.py) at the
+    Euler points where the FP64 sequence is worst; the GPU must be within 1e-10 of it."""
     import os
     d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ti48_highprec.npz"))
     w = ti48

@@ -147,7 +147,7 @@ def test_ge76_kernel_files_through_gpu(ge76, form):
 
 
 def test_df64_form_energies_within_1kev_of_fp64():
-    """Every form must keep E_J and GCM levels within 1 keV of FP64 (the benchmark spec)."""
+    """Every form must keep E_J and GCM levels within 1 keV of FP64."""
     from sccm_gb300.forms import compare
     w = make_workload("pf", 4, Mesh(4, 8, 4, 5), seed=606)
     r = compare(w, "df64")
