@@ -162,6 +162,30 @@ def level_weights(kernels, pairs, nvac, jvals=(0, 2, 4, 6), eps=1e-5, nlev=3):
     return out
 
 
+def diagonal_norms(kernels, pairs, jvals=(0, 2, 4, 6)):
+    """max_K |N^J_KK(q, q)| per vacuum q and J, from the diagonal pairs of a pair set."""
+    diag = {}
+    for (i, j), k in zip(pairs, kernels):
+        if i == j:
+            diag[i] = {J: float(np.abs(np.diagonal(k["njkk"][J])).max()) for J in jvals}
+    return diag
+
+
+def level_error_bound(W, pairs, diag, err_norm, jvals=(0, 2, 4, 6)):
+    """First-order bound on the GCM-level / E_J error (in the units of `err_norm`) when every
+    pair's H^J entries carry an error of err_norm in the basis of normalised states, i.e.
+    err_norm x sqrt(N^J(q,q) N^J(q',q')) absolute, the (2J+1)-row block's spectral norm
+    taken as (2J+1) times that. W: `level_weights` of the same pairs."""
+    bound = 0.0
+    for J in jvals:
+        tot = 0.0
+        for p, (i, j) in enumerate(pairs):
+            if i in diag and j in diag:
+                tot += W[J][p] * (2 * J + 1) * err_norm * np.sqrt(diag[i][J] * diag[j][J])
+        bound = max(bound, tot)
+    return float(bound)
+
+
 def assemble(kernels, pairs, nvac, J, field):
     """Matrix over (q, K) of one projected field for angular momentum J."""
     d = 2 * J + 1

@@ -478,23 +478,11 @@ class LearnedPNAMP:
         taken at the level the flagging aims for (flag_kev in the basis of normalised states,
         times sqrt(N^J(q,q) N^J(q',q')) from the coarse diagonal norms), so the bound is what
         the mode achieves at best. Returns (bound in keV, coarse kernels)."""
-        from .gcm import level_weights
+        from .gcm import diagonal_norms, level_error_bound, level_weights
         ck = self.coarse_kernels(pairs)
         W = level_weights(ck, pairs, nvac, jvals, eps, nlev)
-        diag = {}
-        for r in ck:
-            i, j = r["pair"]
-            if i == j:
-                diag[i] = {J: float(np.abs(np.diagonal(r["njkk"][J])).max()) for J in jvals}
-        bound = 0.0
-        for J in jvals:
-            tot = 0.0
-            for p, (i, j) in enumerate(pairs):
-                if i in diag and j in diag:
-                    sc = math.sqrt(diag[i][J] * diag[j][J])
-                    tot += W[J][p] * (2 * J + 1) * self.cfg.flag_kev * 1e-3 * sc
-            bound = max(bound, tot)
-        return bound * 1e3, ck
+        bound = level_error_bound(W, pairs, diagonal_norms(ck, pairs, jvals), self.cfg.flag_kev, jvals)
+        return bound, ck
 
     def run_gcm(self, pairs, nvac, jvals=(0, 2, 4, 6), eps=1e-5, nlev=3, exact_ctx=None, train_pairs=None):
         """`run` over the complete pair set of `nvac` vacua, then the Hill-Wheeler gate.

@@ -3,7 +3,7 @@ level weights the learned mode's Hill-Wheeler gate uses (no GPU)."""
 import numpy as np
 
 from sccm_gb300.basis import JJMAX
-from sccm_gb300.gcm import gcm_levels, hndiag, level_weights
+from sccm_gb300.gcm import diagonal_norms, gcm_levels, hndiag, level_error_bound, level_weights
 
 
 def _random_kernels(nvac, jvals, rng, small=1e-4):
@@ -85,3 +85,35 @@ def test_level_weights_grow_with_norm_conditioning():
     rng = np.random.default_rng(3)
     w_bad = level_weights(*_random_kernels(3, (0,), rng, small=1e-4), 3, (0,))
     assert w_bad[0].max() > 10 * w_ok[0].max()
+
+
+def test_level_error_bound_covers_errors_of_that_size():
+    """Errors of a given size in the basis of normalised states on every pair's H^J entries
+    move the levels and E_J by at most level_error_bound (first order, small errors)."""
+    rng = np.random.default_rng(9)
+    nvac, jvals = 4, (0, 2)
+    ker, pairs = _random_kernels(nvac, jvals, rng)
+    W = level_weights(ker, pairs, nvac, jvals, nlev=3)
+    diag = diagonal_norms(ker, pairs, jvals)
+    err = 1e-8
+    bound = level_error_bound(W, pairs, diag, err, jvals)
+    base = gcm_levels(ker, pairs, nvac, jvals)
+    for trial in range(3):
+        pert = []
+        for k, (i, j) in enumerate(pairs):
+            r = {f: v.copy() for f, v in ker[k].items()}
+            for J in jvals:
+                d = 2 * J + 1
+                sl = slice(JJMAX - J, JJMAX + J + 1)
+                sc = np.sqrt(diag[i][J] * diag[j][J])
+                ph = np.exp(2j * np.pi * rng.uniform(size=(d, d)))
+                D = err * sc * ph            # every entry exactly err in normalised units
+                if i == j:
+                    D = 0.5 * (D + D.conj().T)
+                r["hjkk"][J, sl, sl] += D
+            pert.append(r)
+        got = gcm_levels(pert, pairs, nvac, jvals)
+        for J in jvals:
+            dl = np.abs(got[J]["levels"][:3] - base[J]["levels"][:3]).max()
+            dq = np.abs(got[J]["per_q"] - base[J]["per_q"]).max()
+            assert max(dl, dq) <= 1.01 * bound
