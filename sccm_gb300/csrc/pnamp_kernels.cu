@@ -1,21 +1,28 @@
-// PNAMP kernels for GB300 (sm_103a), FP64.
+// PNAMP kernels for GB300 (sm_103a): the per-point algebra in FP64 (zc) or double-float
+// (zd, float pairs on the FP32 pipes), one template.
 //
 // Work decomposition (one CUDA launch per stage, batched over pairs):
-//   setup_kernel   one CTA per (q,q') pair: W = V1 U1^-1, Z0 = V0 U0^-1 and the
-//                  bare-vacuum overlaps det(1 + Z^T Z)^(-1/4)
-//                  (reference: zbareover, Codes/PNAMP/PNAMP_Proj.f90:6-79).
+//   setup_kernel   one CTA per (q,q') pair: W = V1 U1^-1, Z0 = V0 U0^-1, the
+//                  bare-vacuum overlaps det(1 + Z^T Z)^(-1/4) (zbareover,
+//                  Codes/PNAMP/PNAMP_Proj.f90:6-79), and the once-per-pair pieces of
+//                  the reduced Pfaffian (Z0^-1, Pf(-c Z0)) and the species-split flag.
 //   point_kernel   persistent; one CTA per (pair, Euler point) work item at a
 //                  time. Per Euler point it builds the block-diagonal Wigner-D
 //                  rotation R (ROTATION_MAT, PNAMP_Proj.f90:83-136) and the
 //                  gauge-independent pieces X = R W R^T, R V1, R* U1 and the four
-//                  species partials of T22; then for each of the NFOM^2 gauge
-//                  points: the Pfaffian of Cscale [[D X D, -I], [I, -Z0]] with the
-//                  reference's pivoting and sign (Pfaf_Over + ZPfaffianF + ZExch,
-//                  PNAMP_Proj.f90:142-392), the LU of T22 and two row solves
-//                  giving rho, kappa10, kappa01 (ROKAPPAphiomega, :459-551), and
-//                  the observables of Kernel3D.f90:296-358 (ZN_0, the energy of
-//                  PNAMP_Energy_OpenMP.f90:31-90, ZJ2_0, ZQ2/ZQ2t), summed into
-//                  ZRES(iang, io) (Kernel3D.f90:385-387).
+//                  species partials of T22; then for each of the NFOM^2 gauge points:
+//                  the Pfaffian of the point's skew matrix (Pfaf_Over + ZPfaffianF +
+//                  ZExch, PNAMP_Proj.f90:142-392; the n x n Schur complement c (D X D -
+//                  Z0^-1) when V0 is well conditioned, two h x h species blocks for
+//                  charge-conserving pairs, else the 2n x 2n matrix) beside the column
+//                  Gauss-Jordan solve Y T22^-1 on other warps (named barriers), then
+//                  rho, kappa10, kappa01 (ROKAPPAphiomega, :459-551) and the observables
+//                  of Kernel3D.f90:296-358 (ZN_0, the energy of
+//                  PNAMP_Energy_OpenMP.f90:31-90 or the split-bf16 rows for the tensor-
+//                  core contraction in contract_tc.cu, ZJ2_0, ZQ2/ZQ2t), summed into
+//                  ZRES(iang, io) (Kernel3D.f90:385-387). Species-split pairs run two
+//                  gauge points at a time on the two halves of the CTA
+//                  (split_pair_points) with compact species-block densities.
 //   project_kernel J/K projection of ZRES (Kernel3D.f90:415-751, plain form of
 //                  PNAMP_Kernel3D_v2.f90:477-498).
 //
