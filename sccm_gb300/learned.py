@@ -27,6 +27,10 @@ this mode instead
     of the learned H^J (`gcm.level_weights`). Pairs are sent to the full mesh,
     largest weight x estimated block error first, until the bound on the level
     error left is below `gcm_safety` x `gcm_kev`.
+`run_gcm` first takes the same weights from the coarse-mesh kernels alone
+(`precheck`): when even the error the flagging aims for would leave more than
+`gcm_kev` on the levels, it computes every pair on the full mesh at once, before
+any training, norm pass or network work.
 
 Errors are measured in the basis of normalised states: an error dH in
 H^J(q, q') is taken relative to sqrt(N^J(q, q) N^J(q', q')), the diagonal
