@@ -176,13 +176,20 @@ def test_pf_case_mesh_sample_matches_oracle(cfg1, form):
     assert np.abs(z[0][others]).max() == 0.0   # items not listed are not written
 
 
+@pytest.fixture(scope="module")
+def pfsplit():
+    return make_workload("pf", 2, Mesh(2, 3, 2, 3), seed=202)
+
+
 @pytest.mark.parametrize("form", FORMS)
-def test_pfaffian_early_exit_value_and_status(pfmix, form):
+@pytest.mark.parametrize("which", ["pfmix", "pfsplit"])
+def test_pfaffian_early_exit_value_and_status(which, form, request):
     """A Pfaffian matrix scale (Input%Cscale) so small that every pivot is below the
     reference's 1e-13 (PNAMP_Proj.f90:290,333): the oracle's ZPfaffianF returns 0 with its
     exit flag at the first step, and the GPU must give N = 0 (hence ZRES = 0) with
-    PNAMP_ST_PIVOT_UNDERFLOW at every Euler point."""
-    w = pfmix
+    PNAMP_ST_PIVOT_UNDERFLOW at every Euler point; for proton-neutron-mixing vacua (the
+    general path) and for species-split ones (two gauge points per CTA)."""
+    w = request.getfixturevalue(which)
     cscale = 1e-16
     ham = Hamiltonian(w.e0, w.t1b, w.recs, w.vbar, w.q2, w.jops)
     log = []
